@@ -1,0 +1,322 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 SGM engine on configuration A (1920x1080, D=64,
+4 paths, bit-exact), in MDE/s (W*H*D / second), with frames/s beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step is one frame through the engine. `value` is measured with the
+inputs already resident on the device (one CUDA-graph launch per frame,
+round-robin over 8 distinct synthetic pairs); `e2e` is the same metric
+through the host-buffer call (sgmgb_run_frame: pinned host inputs copied in,
+the disparity map copied back, every step). `roofline` relates the modelled
+minimal bytes of a frame (2*W*H*D + 3*W*H) to its device time and the
+measured HBM copy bandwidth. `cpu_baseline` is the CPU oracle on a bounded
+sample of the same workload, one thread. `--impl reference` times the CPU
+oracle (the reference's algorithm, restated in C) on all host threads.
+
+Multi-GPU: frames are independent, so N GPUs run N replicas (one process per
+GPU under torchrun); `value` is the frames of all ranks over the slowest
+rank's time. No collective is on the data path.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "sgm-bench_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+W, H, D, PATHS = 1920, 1080, 64, 4
+WORKLOAD = "configA_1920x1080_D64_4path"
+METRIC = "MDE/s (W*H*D per second), 1080p D=64 4-path, bit-exact"
+UNIT = "MDE/s"
+B_ALG = 2 * W * H * D + 3 * W * H          # modelled minimal bytes per frame
+KERNELS_PER_FRAME = 1 + PATHS               # census + one pass per direction
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per frame from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "configA_frame_traffic.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_frame:"):
+                return int(line.split(":")[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self, t0, t1):
+        rows = [r for (ts, r) in self.rows if t0 - 0.06 <= ts <= t1 + 0.06] or [r for _, r in self.rows[-2:]]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        sm = []
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+            except ValueError:
+                pass
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        try:
+            smax = float(rows[0][2])
+        except ValueError:
+            smax = None
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline_sample(seconds=12.0):
+    """The oracle, one thread, on whole frames of the workload (at least one)."""
+    import oracle
+    import sgmgb
+    left, right, _ = sgmgb.synth_pair(W, H, D, 101)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        oracle.plain(left, right, D, PATHS)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 8:
+            break
+    return {"value": n * W * H * D / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d frame(s) of %dx%d D=%d %d-path, oracle/sgm_oracle.c, 1 thread, %.1f s"
+                      % (n, W, H, D, PATHS, el)}
+
+
+def run_reference(args):
+    """The reference's CPU algorithm (oracle port) on every host thread."""
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    import concurrent.futures as cf
+    import oracle
+    import sgmgb
+    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    # each step: every thread runs one band of the frame (a full frame when the
+    # run is short); rows scale down so the whole run stays within minutes.
+    rows = max(64, min(H, int(H * 16 / max(16, args.steps + args.warmup))))
+    pairs = [sgmgb.synth_pair(W, H, D, 200 + t) for t in range(threads)]
+    bands = [(l[:rows].copy(), r[:rows].copy()) for l, r, _ in pairs]
+    pool = cf.ThreadPoolExecutor(max_workers=threads)
+
+    def step():
+        list(pool.map(lambda lr: oracle.plain(lr[0], lr[1], D, PATHS), bands))
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = time.perf_counter() - t0
+    per_step = el / args.steps
+    value = threads * W * rows * D / per_step / 1e6
+    sample = "%d threads x one %dx%d D=%d %d-path band per step (oracle port of common/sgm_ref.c)" % (
+        threads, W, rows, D, PATHS)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "W": W, "H": H, "D": D, "paths": PATHS,
+                       "sample_rows": rows, "threads": threads},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    import sgmgb
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    eng = sgmgb.Engine(local)
+    eng.plan(W, H, D, PATHS)
+    # 8 distinct resident pairs, round-robin: inputs differ every step and the
+    # per-frame working set (about 430 MB of census, scratch and sum planes)
+    # is far larger than the 129 MB L2.
+    R = 8
+    pairs = [sgmgb.synth_pair(W, H, D, 1000 * rank + k + 1) for k in range(R)]
+    dl = [torch.from_numpy(p[0]).to(dev) for p in pairs]
+    dr = [torch.from_numpy(p[1]).to(dev) for p in pairs]
+    dd = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(R)]
+    s = torch.cuda.current_stream(dev)
+
+    # correctness of what is timed: the first pair against the oracle (rank 0)
+    eng.run_frame_async(dl[0], dr[0], dd[0], stream=s)
+    s.synchronize()
+    bit_exact = None
+    if rank == 0:
+        import oracle
+        bit_exact = bool(np.array_equal(dd[0].cpu().numpy(), oracle.plain(pairs[0][0], pairs[0][1], D, PATHS)))
+
+    for i in range(args.warmup):
+        eng.run_frame_async(dl[i % R], dr[i % R], dd[i % R], stream=s)
+    s.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    tw0 = time.time()
+    ev0.record(s)
+    for i in range(args.steps):
+        eng.run_frame_async(dl[i % R], dr[i % R], dd[i % R], stream=s)
+    ev1.record(s)
+    barrier()
+    tw1 = time.time()
+    clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = ws * args.steps * W * H * D / (ms / 1e3) / 1e6
+
+    # end to end through the host-buffer call: pinned inputs in, map out, every step
+    hl = [torch.from_numpy(p[0]).pin_memory().numpy() for p in pairs]
+    hr = [torch.from_numpy(p[1]).pin_memory().numpy() for p in pairs]
+    e2e_steps = max(3, min(args.steps, 200))
+    for i in range(3):
+        eng.run_frame(hl[i % R], hr[i % R])
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    lat = []
+    for i in range(e2e_steps):
+        a = time.perf_counter()
+        eng.run_frame(hl[i % R], hr[i % R])
+        lat.append(time.perf_counter() - a)
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = ws * e2e_steps * W * H * D / e2e_s / 1e6
+    _, st = eng.run_frame(hl[0], hr[0], times=True)
+
+    if rank != 0:
+        eng.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    peak, peak_kind = peaks()
+    achieved = B_ALG / (ms_per_step / 1e3) / 1e9
+    traffic = committed_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u16", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "W": W, "H": H, "D": D, "paths": PATHS, "variant": "plain",
+                   "inputs": "8 resident synthetic pairs round-robin; per-frame working set ~430 MB > L2",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "fps": ws * args.steps / (ms / 1e3),
+        "bit_exact_vs_oracle": bit_exact,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * W * H, "d2h_bytes_per_step": W * H,
+                "fps": ws * e2e_steps / e2e_s, "p50_ms": statistics.median(lat) * 1e3,
+                "p99_ms": sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
+                "stage_ms": {k: round(v, 4) for k, v in st.items() if k.endswith("_ms")}},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "note": "one launch = one CUDA-graph launch of the frame pipeline (census + %d path "
+                             "passes); achieved = %d modelled bytes / device time; peak %s" % (
+                                 PATHS, B_ALG, peak_kind)},
+        "cpu_baseline": cpu_baseline_sample(args.cpu_seconds),
+        "clocks": clocks.summary(tw0, tw1),
+        "gpu_launches": args.steps * KERNELS_PER_FRAME,
+    }
+    print(json.dumps(line))
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

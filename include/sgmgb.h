@@ -1,0 +1,175 @@
+/* sgmgb.h -- C ABI of the GB300 SGM stereo engine (libsgmgb.so).
+ *
+ * Plain pointers and sizes only. Every entry point returns SGMGB_OK (0) or a
+ * negative SGMGB_ERR_* code; sgmgb_strerror() names the code and
+ * sgmgb_last_error() gives the message of the last failure on a context.
+ *
+ * Algorithms (bit-exact with kylefoxaustin/sgm-bench):
+ *   SGMGB_PLAIN       census 9x7 -> Hamming cost (invalid 62) -> 4 or 8 paths,
+ *                     P1 = 20, P2 = 192 -> argmin, lowest d on ties
+ *                     (common/sgm_ref.c:101-144). D: multiple of 16 in [16, 256].
+ *   SGMGB_MULTISCALE  SobelX -> census at 1/2 and full resolution -> averaged
+ *                     cost (invalid 63) -> 8 paths with P1 40/20/10, P2 = 200,
+ *                     saturating -> argmin at (2x,2y) (multiscale/sgm_ms_ref.c:
+ *                     151-200). D = 64 and paths = 8 only; W and H even.
+ *                     The output map is (W/2) x (H/2).
+ *
+ * Reference interfaces each group replaces:
+ *   sgmgb_run_frame       the single-frame sgm_run_fn (common/sgm.h:29-31) as
+ *                         used by the harness loops (common/harness.c:150-158);
+ *                         sgm_gb300.c wraps it as SGM_IMPL.
+ *   sgmgb_run_frame_async the device half of cuda_run (cuda/sgm_cuda_opt.cu:
+ *                         321-366): inputs already on the device, one stream.
+ *   sgmgb_ms_run          the standalone multi-scale binary's frame loop
+ *                         (multiscale/sgm_ms_ref.c:166-202).
+ *   sgmgb_batch_*         no reference symbol: many frames per launch.
+ *   sgmgb_server_*        no reference symbol: a continuous-batching request loop.
+ */
+#ifndef SGMGB_H
+#define SGMGB_H
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGMGB_ABI_VERSION 1
+
+enum {
+    SGMGB_OK          = 0,
+    SGMGB_ERR_ARG     = -1,   /* bad size, D, path count, variant or pointer */
+    SGMGB_ERR_NOMEM   = -2,   /* host or device allocation failed */
+    SGMGB_ERR_CUDA    = -3,   /* a CUDA call failed; see sgmgb_last_error */
+    SGMGB_ERR_NODEV   = -4,   /* no usable CUDA device */
+    SGMGB_ERR_BUDGET  = -5,   /* request refused: over the HBM budget or no free slot */
+    SGMGB_ERR_TIMEOUT = -6,   /* a bounded device or host wait ran out */
+    SGMGB_ERR_STATE   = -7    /* call not valid in the current state */
+};
+
+enum { SGMGB_PLAIN = 0, SGMGB_MULTISCALE = 1 };
+
+/* Same layout as sgm_stage_times (include/sgm_plugin.h). */
+typedef struct {
+    double census_ms;
+    double cost_ms;
+    double aggregate_ms;
+    double argmin_ms;
+    double transfer_ms;
+    int    threads_used;
+} sgmgb_stage_times;
+
+typedef struct {
+    int W, H;      /* input size in pixels */
+    int D;         /* disparity range */
+    int paths;     /* 4 or 8 */
+    int variant;   /* SGMGB_PLAIN or SGMGB_MULTISCALE */
+} sgmgb_frame_desc;
+
+typedef struct sgmgb_ctx sgmgb_ctx;
+
+/* ---- version, errors, sizes (no GPU needed) ---- */
+int         sgmgb_abi_version(void);
+const char *sgmgb_strerror(int code);
+const char *sgmgb_last_error(const sgmgb_ctx *ctx);
+/* Validates a frame description (SGMGB_OK or SGMGB_ERR_ARG). */
+int         sgmgb_check_desc(const sgmgb_frame_desc *fd);
+/* Output map size: W x H for plain, (W/2) x (H/2) for multi-scale. */
+int         sgmgb_out_size(const sgmgb_frame_desc *fd, int *out_w, int *out_h);
+/* Device bytes one frame slot of this description holds resident. */
+int         sgmgb_workspace_bytes(const sgmgb_frame_desc *fd, size_t *bytes);
+
+/* ---- context ---- */
+/* Binds to CUDA device `device`; fails with SGMGB_ERR_NODEV without one. */
+int  sgmgb_create(int device, sgmgb_ctx **out);
+void sgmgb_destroy(sgmgb_ctx *ctx);
+/* Sizes the context's resident single-frame workspace (re-plans on change). */
+int  sgmgb_plan(sgmgb_ctx *ctx, const sgmgb_frame_desc *fd);
+
+/* ---- single frame ---- */
+/* Host buffers in and out, synchronous: the drop-in call. left/right are
+ * W*H bytes, row-major; disp receives the output map (sgmgb_out_size). */
+int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right,
+                    uint8_t *disp, sgmgb_stage_times *t);
+/* Device buffers, enqueued on `stream` (a cudaStream_t, NULL = the context's
+ * own stream); returns without waiting. Uses the planned workspace. */
+int sgmgb_run_frame_async(sgmgb_ctx *ctx, const uint8_t *d_left, const uint8_t *d_right,
+                          uint8_t *d_disp, void *stream);
+/* Waits for everything the context enqueued on `stream` (NULL = own stream). */
+int sgmgb_sync(sgmgb_ctx *ctx, void *stream);
+
+/* ---- component entry points (parity tests, tools) ---- */
+/* 9x7 census of one W x H image on the device; out is W*H uint64. */
+int sgmgb_census_async(sgmgb_ctx *ctx, const uint8_t *d_img, uint64_t *d_out, int W, int H,
+                       void *stream);
+
+/* ---- batch: many frames of mixed sizes in one persistent launch ---- */
+typedef struct sgmgb_batch sgmgb_batch;
+/* Plans n frames: workspace per frame, the per-frame tile queue, the tile
+ * shape (autotuned per frame shape and cached), and a CUDA graph of the
+ * whole batch. */
+int  sgmgb_batch_create(sgmgb_ctx *ctx, const sgmgb_frame_desc *frames, int n,
+                        sgmgb_batch **out);
+/* Runs the planned batch on device buffers (arrays of n pointers, host
+ * arrays of device pointers). Enqueued on `stream`; returns without waiting. */
+int  sgmgb_batch_run(sgmgb_batch *b, const uint8_t *const *d_left,
+                     const uint8_t *const *d_right, uint8_t *const *d_disp, void *stream);
+/* Tile shape chosen for frame i: warps per block and lines per tile. */
+int  sgmgb_batch_tile_shape(const sgmgb_batch *b, int i, int *warps_per_block,
+                            int *lines_per_tile);
+void sgmgb_batch_destroy(sgmgb_batch *b);
+
+/* ---- autotuner cache (host-only; no GPU needed) ---- */
+/* Records / looks up the chosen tile shape for a frame shape. The cache file
+ * is a plain text table "W H D paths variant warps lines us". */
+int sgmgb_tune_lookup(const char *cache_path, const sgmgb_frame_desc *fd,
+                      int *warps_per_block, int *lines_per_tile);
+int sgmgb_tune_record(const char *cache_path, const sgmgb_frame_desc *fd,
+                      int warps_per_block, int lines_per_tile, double us);
+
+/* ---- server: continuous batching of camera frames ---- */
+typedef struct sgmgb_server sgmgb_server;
+typedef struct {
+    size_t hbm_budget_bytes;   /* admission limit for resident workspaces */
+    int    max_inflight;       /* frames on the device at once */
+    int    streams;            /* CUDA streams the frames are spread over */
+} sgmgb_server_config;
+typedef struct {
+    uint64_t frames_done;
+    uint64_t frames_refused;
+    double   p50_ms, p99_ms, max_ms;   /* submit -> result on the host */
+    double   fps;                      /* frames_done / wall time */
+    size_t   resident_bytes;
+} sgmgb_server_stats;
+
+int  sgmgb_server_create(sgmgb_ctx *ctx, const sgmgb_server_config *cfg,
+                         sgmgb_server **out);
+/* Registers a camera: allocates its resident buffers if the budget allows
+ * (SGMGB_ERR_BUDGET otherwise). */
+int  sgmgb_server_add_camera(sgmgb_server *s, int cam_id, const sgmgb_frame_desc *fd);
+/* Submits one frame (host buffers of W*H bytes, copied before returning).
+ * Admitted frames join the device work immediately; *ticket identifies it.
+ * SGMGB_ERR_BUDGET when no slot is free for this camera. */
+int  sgmgb_server_submit(sgmgb_server *s, int cam_id, const uint8_t *left,
+                         const uint8_t *right, uint64_t *ticket);
+/* Non-blocking: 1 and the output map (and latency) when done, 0 if pending. */
+int  sgmgb_server_poll(sgmgb_server *s, uint64_t ticket, uint8_t *disp, double *latency_ms);
+/* Blocks up to timeout_ms for the ticket (SGMGB_ERR_TIMEOUT when it runs out). */
+int  sgmgb_server_wait(sgmgb_server *s, uint64_t ticket, uint8_t *disp, double *latency_ms,
+                       int timeout_ms);
+int  sgmgb_server_stats_get(sgmgb_server *s, sgmgb_server_stats *st);
+void sgmgb_server_destroy(sgmgb_server *s);
+
+/* ---- synthetic stereo pairs (host-only, deterministic on every CPU) ---- */
+/* Band-limited noise (Gaussian-blurred uniform octaves, sigma 1/4/16),
+ * ground truth piecewise planar over 40 Voronoi cells (offsets in [0, D-1],
+ * slopes within +-0.02 px/px), right = left warped by the ground truth with
+ * occlusions refilled from fresh noise, plus Gaussian noise sigma 2.
+ * Writes W*H bytes to each non-NULL output. */
+int sgmgb_synth_pair(int W, int H, int D, uint64_t seed, uint8_t *left, uint8_t *right,
+                     uint8_t *gt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

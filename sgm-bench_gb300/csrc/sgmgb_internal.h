@@ -1,0 +1,64 @@
+// sgmgb_internal.h -- host-side structures shared by the runtime, batch and server files.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include "../../include/sgmgb.h"
+#include "sgmgb_kernels.cuh"
+
+struct sgmgb_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    // resident single-frame workspace (sgmgb_plan)
+    sgmgb_frame_desc fd{};
+    bool planned = false;
+    struct FrameSlot *slot = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // CUDA graphs of the planned frame pipeline, one per (left, right, disp)
+    // pointer triple seen (a small round-robin cache); replayed by
+    // sgmgb_run_frame_async, all dropped when the plan changes.
+    static constexpr int kGraphs = 8;
+    cudaGraphExec_t graph[kGraphs] = {};
+    const void *graph_key[kGraphs][3] = {};
+    int graph_next = 0;
+    int warps_per_block = 4;
+};
+
+// Device buffers of one frame slot. All pointers are carved from one
+// allocation (`base`), 256-byte aligned.
+struct FrameSlot {
+    sgmgb_frame_desc fd{};
+    void *base = nullptr;
+    size_t bytes = 0;
+    uint8_t *left = nullptr, *right = nullptr, *disp = nullptr;   // inputs / output
+    uint64_t *cl = nullptr, *cr = nullptr;                        // full-scale census
+    uint8_t *sc = nullptr;                                        // W*H*D scratch L
+    uint16_t *S = nullptr;                                        // W*H*D sum
+    // multi-scale extras
+    uint8_t *sobL = nullptr, *sobR = nullptr;                     // full-scale SobelX
+    uint8_t *halfL = nullptr, *halfR = nullptr;                   // half-scale images
+    uint8_t *hsobL = nullptr, *hsobR = nullptr;                   // half-scale SobelX
+    uint64_t *cl1 = nullptr, *cr1 = nullptr;                      // half-scale census
+    uint8_t *disp1 = nullptr;                                     // stage-1 argmin (defined work, unused)
+};
+
+namespace sgmgb {
+
+// Byte layout of a slot for a frame description; total in *bytes.
+size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s /* may be null: size only */);
+int  slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err);
+void slot_free(FrameSlot *s);
+
+// Enqueues the whole frame pipeline for `s` reading d_left/d_right and
+// writing d_disp on `st`. Events ev_census / ev_agg (optional) are recorded
+// after the census phase and at the end. warps_per_block: path-kernel shape.
+cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8_t *d_right,
+                          uint8_t *d_disp, cudaStream_t st, int warps_per_block,
+                          cudaEvent_t ev_census, cudaEvent_t ev_end);
+
+int set_err(sgmgb_ctx *ctx, int code, const std::string &msg);
+
+}  // namespace sgmgb

@@ -1,0 +1,372 @@
+// sgmgb_runtime.cu -- context, resident workspace, frame pipeline and the
+// single-frame entry points of the C ABI (include/sgmgb.h).
+#include "sgmgb_internal.h"
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+using namespace sgmgb;
+
+namespace sgmgb {
+
+int set_err(sgmgb_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
+    const size_t W = (size_t)fd.W, H = (size_t)fd.H, D = (size_t)fd.D, N = W * H;
+    size_t off = 0;
+    auto take = [&](size_t n) { size_t o = off; off += al256(n); return o; };
+    const size_t o_left = take(N), o_right = take(N);
+    const size_t out_n = fd.variant == SGMGB_MULTISCALE ? (W / 2) * (H / 2) : N;
+    const size_t o_disp = take(out_n);
+    const size_t o_cl = take(N * 8), o_cr = take(N * 8);
+    const size_t o_sc = take(N * D), o_S = take(N * D * 2);
+    size_t o_sobL = 0, o_sobR = 0, o_hL = 0, o_hR = 0, o_hsL = 0, o_hsR = 0, o_cl1 = 0, o_cr1 = 0, o_d1 = 0;
+    if (fd.variant == SGMGB_MULTISCALE) {
+        const size_t Nh = (W / 2) * (H / 2);
+        o_sobL = take(N); o_sobR = take(N);
+        o_hL = take(Nh); o_hR = take(Nh); o_hsL = take(Nh); o_hsR = take(Nh);
+        o_cl1 = take(Nh * 8); o_cr1 = take(Nh * 8);
+        o_d1 = take(Nh);
+    }
+    if (s) {
+        uint8_t *b = (uint8_t *)s->base;
+        s->left = b + o_left; s->right = b + o_right; s->disp = b + o_disp;
+        s->cl = (uint64_t *)(b + o_cl); s->cr = (uint64_t *)(b + o_cr);
+        s->sc = b + o_sc; s->S = (uint16_t *)(b + o_S);
+        if (fd.variant == SGMGB_MULTISCALE) {
+            s->sobL = b + o_sobL; s->sobR = b + o_sobR;
+            s->halfL = b + o_hL; s->halfR = b + o_hR; s->hsobL = b + o_hsL; s->hsobR = b + o_hsR;
+            s->cl1 = (uint64_t *)(b + o_cl1); s->cr1 = (uint64_t *)(b + o_cr1);
+            s->disp1 = b + o_d1;
+        }
+    }
+    return off;
+}
+
+int slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err) {
+    FrameSlot *s = new (std::nothrow) FrameSlot();
+    if (!s) { err = "host allocation failed"; return SGMGB_ERR_NOMEM; }
+    s->fd = fd;
+    s->bytes = slot_layout(fd, nullptr);
+    cudaError_t e = cudaMalloc(&s->base, s->bytes);
+    if (e != cudaSuccess) {
+        err = std::string("cudaMalloc of ") + std::to_string(s->bytes) + " bytes: " + cudaGetErrorString(e);
+        cudaGetLastError();
+        delete s;
+        return SGMGB_ERR_NOMEM;
+    }
+    slot_layout(fd, s);
+    *out = s;
+    return SGMGB_OK;
+}
+
+void slot_free(FrameSlot *s) {
+    if (!s) return;
+    if (s->base) cudaFree(s->base);
+    delete s;
+}
+
+// Pass schedule. Opposite directions are paired: the first of a pair parks
+// its L in the scratch plane, the second adds both into S; the last pass
+// also takes the argmin. Directions and penalties follow common/sgm_ref.c:
+// 96-99 (plain, P1 = 20 for all) and multiscale/sgm_ms_ref.c:85-87 (P1 40
+// horizontal, 20 vertical, 10 diagonal).
+struct PassSpec { int dx, dy, mode; };
+static const PassSpec kPasses4[4] = {
+    {-1, 0, MODE_SCRATCH}, {1, 0, MODE_STORE}, {0, -1, MODE_SCRATCH}, {0, 1, MODE_FINAL}};
+static const PassSpec kPasses8[8] = {
+    {-1, 0, MODE_SCRATCH}, {1, 0, MODE_STORE}, {0, -1, MODE_SCRATCH}, {0, 1, MODE_ACCUM},
+    {-1, -1, MODE_SCRATCH}, {1, 1, MODE_ACCUM}, {1, -1, MODE_SCRATCH}, {-1, 1, MODE_FINAL}};
+
+static int ms_p1(int dx, int dy) { return dy == 0 ? 40 : (dx == 0 ? 20 : 10); }
+
+static cudaError_t run_paths(const LineParams &base, int paths, int cost_kind, int sat, bool ms,
+                             int wpb, cudaStream_t st) {
+    const PassSpec *ps = paths == 8 ? kPasses8 : kPasses4;
+    for (int i = 0; i < paths; i++) {
+        LineParams p = base;
+        p.dx = ps[i].dx; p.dy = ps[i].dy;
+        p.p1 = ms ? ms_p1(p.dx, p.dy) : 20;
+        p.nlines = lines_for(p.W, p.H, p.dx, p.dy);
+        cudaError_t e = launch_line(p, ps[i].mode, cost_kind, sat, wpb, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8_t *d_right,
+                          uint8_t *d_disp, cudaStream_t st, int wpb, cudaEvent_t ev_census,
+                          cudaEvent_t ev_end) {
+    const sgmgb_frame_desc &fd = s.fd;
+    cudaError_t e;
+    if (fd.variant == SGMGB_PLAIN) {
+        if ((e = launch_census2(d_left, d_right, s.cl, s.cr, fd.W, fd.H, st)) != cudaSuccess) return e;
+        if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
+        LineParams p{};
+        p.cl = s.cl; p.cr = s.cr; p.sc = s.sc; p.S = s.S; p.disp = d_disp;
+        p.W = fd.W; p.H = fd.H; p.D = fd.D; p.nl = fd.D / dpl_for(fd.D);
+        p.p2 = 192; p.even_only = 0;
+        if ((e = run_paths(p, fd.paths, COST_PLAIN, 0, false, wpb, st)) != cudaSuccess) return e;
+    } else {
+        const int W = fd.W, H = fd.H, hw = W / 2, hh = H / 2;
+        // stage 1: half scale (multiscale/sgm_ms_ref.c:168-181)
+        if ((e = launch_half2(d_left, d_right, s.halfL, s.halfR, W, H, st)) != cudaSuccess) return e;
+        if ((e = launch_sobel2(s.halfL, s.halfR, s.hsobL, s.hsobR, hw, hh, st)) != cudaSuccess) return e;
+        if ((e = launch_census2(s.hsobL, s.hsobR, s.cl1, s.cr1, hw, hh, st)) != cudaSuccess) return e;
+        if ((e = launch_sobel2(d_left, d_right, s.sobL, s.sobR, W, H, st)) != cudaSuccess) return e;
+        if ((e = launch_census2(s.sobL, s.sobR, s.cl, s.cr, W, H, st)) != cudaSuccess) return e;
+        if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
+        LineParams p1{};
+        p1.cl = s.cl1; p1.cr = s.cr1; p1.sc = s.sc; p1.S = s.S; p1.disp = s.disp1;
+        p1.W = hw; p1.H = hh; p1.D = 64; p1.nl = 32; p1.p2 = 200; p1.even_only = 0;
+        if ((e = run_paths(p1, 8, COST_MS1, 1, true, wpb, st)) != cudaSuccess) return e;
+        // stage 2: full scale, cost averaged with the half-scale cost (:183-199)
+        LineParams p2{};
+        p2.cl = s.cl; p2.cr = s.cr; p2.cl1 = s.cl1; p2.cr1 = s.cr1; p2.sc = s.sc; p2.S = s.S;
+        p2.disp = d_disp;
+        p2.W = W; p2.H = H; p2.D = 64; p2.nl = 32; p2.p2 = 200; p2.even_only = 1;
+        if ((e = run_paths(p2, 8, COST_MS2, 1, true, wpb, st)) != cudaSuccess) return e;
+    }
+    if (ev_end && (e = cudaEventRecord(ev_end, st)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+}  // namespace sgmgb
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+static void drop_graph(sgmgb_ctx *ctx);
+
+int sgmgb_abi_version(void) { return SGMGB_ABI_VERSION; }
+
+const char *sgmgb_strerror(int code) {
+    switch (code) {
+    case SGMGB_OK: return "ok";
+    case SGMGB_ERR_ARG: return "invalid argument";
+    case SGMGB_ERR_NOMEM: return "out of memory";
+    case SGMGB_ERR_CUDA: return "CUDA error";
+    case SGMGB_ERR_NODEV: return "no CUDA device";
+    case SGMGB_ERR_BUDGET: return "refused: over the HBM budget or no free slot";
+    case SGMGB_ERR_TIMEOUT: return "wait timed out";
+    case SGMGB_ERR_STATE: return "invalid state";
+    default: return "unknown error";
+    }
+}
+
+const char *sgmgb_last_error(const sgmgb_ctx *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int sgmgb_check_desc(const sgmgb_frame_desc *fd) {
+    if (!fd) return SGMGB_ERR_ARG;
+    if (fd->W < 1 || fd->H < 1 || fd->W > 32768 || fd->H > 32768) return SGMGB_ERR_ARG;
+    if (fd->variant == SGMGB_PLAIN) {
+        if (fd->D < 16 || fd->D > 256 || fd->D % 16) return SGMGB_ERR_ARG;
+        if (fd->paths != 4 && fd->paths != 8) return SGMGB_ERR_ARG;
+        return SGMGB_OK;
+    }
+    if (fd->variant == SGMGB_MULTISCALE) {
+        if (fd->D != 64 || fd->paths != 8) return SGMGB_ERR_ARG;
+        if (fd->W < 2 || fd->H < 2 || (fd->W & 1) || (fd->H & 1)) return SGMGB_ERR_ARG;
+        return SGMGB_OK;
+    }
+    return SGMGB_ERR_ARG;
+}
+
+int sgmgb_out_size(const sgmgb_frame_desc *fd, int *out_w, int *out_h) {
+    int rc = sgmgb_check_desc(fd);
+    if (rc) return rc;
+    const bool ms = fd->variant == SGMGB_MULTISCALE;
+    if (out_w) *out_w = ms ? fd->W / 2 : fd->W;
+    if (out_h) *out_h = ms ? fd->H / 2 : fd->H;
+    return SGMGB_OK;
+}
+
+int sgmgb_workspace_bytes(const sgmgb_frame_desc *fd, size_t *bytes) {
+    int rc = sgmgb_check_desc(fd);
+    if (rc) return rc;
+    if (bytes) *bytes = slot_layout(*fd, nullptr);
+    return SGMGB_OK;
+}
+
+int sgmgb_create(int device, sgmgb_ctx **out) {
+    if (!out) return SGMGB_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) { cudaGetLastError(); return SGMGB_ERR_NODEV; }
+    if (device < 0 || device >= n) return SGMGB_ERR_ARG;
+    sgmgb_ctx *ctx = new (std::nothrow) sgmgb_ctx();
+    if (!ctx) return SGMGB_ERR_NOMEM;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        sgmgb_destroy(ctx);
+        return SGMGB_ERR_CUDA;
+    }
+    *out = ctx;
+    return SGMGB_OK;
+}
+
+void sgmgb_destroy(sgmgb_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    slot_free(ctx->slot);
+    for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int sgmgb_plan(sgmgb_ctx *ctx, const sgmgb_frame_desc *fd) {
+    if (!ctx) return SGMGB_ERR_ARG;
+    int rc = sgmgb_check_desc(fd);
+    if (rc) return set_err(ctx, rc, "invalid frame description");
+    if (ctx->planned && !memcmp(&ctx->fd, fd, sizeof *fd)) return SGMGB_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->slot) {
+        cudaStreamSynchronize(ctx->stream);
+        drop_graph(ctx);
+        slot_free(ctx->slot);
+        ctx->slot = nullptr;
+        ctx->planned = false;
+    }
+    std::string err;
+    rc = slot_alloc(*fd, &ctx->slot, err);
+    if (rc) return set_err(ctx, rc, err);
+    ctx->fd = *fd;
+    ctx->planned = true;
+    return SGMGB_OK;
+}
+
+static int cuda_fail(sgmgb_ctx *ctx, cudaError_t e, const char *what) {
+    cudaGetLastError();
+    return set_err(ctx, SGMGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right, uint8_t *disp,
+                    sgmgb_stage_times *t) {
+    if (!ctx || !left || !right || !disp) return SGMGB_ERR_ARG;
+    if (!ctx->planned) return set_err(ctx, SGMGB_ERR_STATE, "sgmgb_plan has not been called");
+    cudaSetDevice(ctx->device);
+    const FrameSlot &s = *ctx->slot;
+    const size_t N = (size_t)s.fd.W * s.fd.H;
+    int ow = 0, oh = 0;
+    sgmgb_out_size(&s.fd, &ow, &oh);
+    const size_t outN = (size_t)ow * oh;
+    using clk = std::chrono::steady_clock;
+    const auto tA = clk::now();
+    cudaError_t e = cudaMemcpyAsync(s.left, left, N, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s.right, right, N, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "host-to-device copy");
+    const auto tB = clk::now();
+    e = cudaEventRecord(ctx->ev[0], ctx->stream);
+    if (e == cudaSuccess)
+        e = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, 4, ctx->ev[1], ctx->ev[2]);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "frame pipeline");
+    const auto tC = clk::now();
+    e = cudaMemcpyAsync(disp, s.disp, outN, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "device-to-host copy");
+    const auto tD = clk::now();
+    if (t) {
+        float census = 0, agg = 0;
+        cudaEventElapsedTime(&census, ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&agg, ctx->ev[1], ctx->ev[2]);
+        t->census_ms = census;
+        t->cost_ms = -1;
+        t->aggregate_ms = agg;
+        t->argmin_ms = -1;
+        t->transfer_ms = std::chrono::duration<double, std::milli>((tB - tA) + (tD - tC)).count();
+        t->threads_used = 0;
+    }
+    return SGMGB_OK;
+}
+
+static void drop_graph(sgmgb_ctx *ctx) {
+    for (int i = 0; i < sgmgb_ctx::kGraphs; i++) {
+        if (ctx->graph[i]) cudaGraphExecDestroy(ctx->graph[i]);
+        ctx->graph[i] = nullptr;
+        ctx->graph_key[i][0] = ctx->graph_key[i][1] = ctx->graph_key[i][2] = nullptr;
+    }
+    ctx->graph_next = 0;
+}
+
+// Captures the frame pipeline for this pointer triple into a CUDA graph on
+// the context's stream (one graph launch per frame afterwards).
+static cudaError_t capture_frame_graph(sgmgb_ctx *ctx, const uint8_t *l, const uint8_t *r, uint8_t *d,
+                                       cudaGraphExec_t *out) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t ee = enqueue_frame(*ctx->slot, l, r, d, ctx->stream, ctx->warps_per_block, nullptr, nullptr);
+    e = cudaStreamEndCapture(ctx->stream, &g);
+    if (ee != cudaSuccess) { if (g) cudaGraphDestroy(g); return ee; }
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    return e;
+}
+
+static cudaError_t frame_graph(sgmgb_ctx *ctx, const uint8_t *l, const uint8_t *r, uint8_t *d,
+                               cudaGraphExec_t *out) {
+    for (int i = 0; i < sgmgb_ctx::kGraphs; i++)
+        if (ctx->graph[i] && ctx->graph_key[i][0] == l && ctx->graph_key[i][1] == r && ctx->graph_key[i][2] == d) {
+            *out = ctx->graph[i];
+            return cudaSuccess;
+        }
+    const int k = ctx->graph_next;
+    ctx->graph_next = (k + 1) % sgmgb_ctx::kGraphs;
+    if (ctx->graph[k]) { cudaGraphExecDestroy(ctx->graph[k]); ctx->graph[k] = nullptr; }
+    cudaError_t e = capture_frame_graph(ctx, l, r, d, &ctx->graph[k]);
+    if (e != cudaSuccess) { ctx->graph[k] = nullptr; return e; }
+    ctx->graph_key[k][0] = l; ctx->graph_key[k][1] = r; ctx->graph_key[k][2] = d;
+    *out = ctx->graph[k];
+    return cudaSuccess;
+}
+
+int sgmgb_run_frame_async(sgmgb_ctx *ctx, const uint8_t *d_left, const uint8_t *d_right,
+                          uint8_t *d_disp, void *stream) {
+    if (!ctx || !d_left || !d_right || !d_disp) return SGMGB_ERR_ARG;
+    if (!ctx->planned) return set_err(ctx, SGMGB_ERR_STATE, "sgmgb_plan has not been called");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaGraphExec_t g = nullptr;
+    cudaError_t e = frame_graph(ctx, d_left, d_right, d_disp, &g);
+    if (e == cudaSuccess) e = cudaGraphLaunch(g, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "frame pipeline");
+    return SGMGB_OK;
+}
+
+int sgmgb_sync(sgmgb_ctx *ctx, void *stream) {
+    if (!ctx) return SGMGB_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaStreamSynchronize(stream ? (cudaStream_t)stream : ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream synchronize");
+    return SGMGB_OK;
+}
+
+int sgmgb_census_async(sgmgb_ctx *ctx, const uint8_t *d_img, uint64_t *d_out, int W, int H,
+                       void *stream) {
+    if (!ctx || !d_img || !d_out || W < 1 || H < 1) return SGMGB_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaError_t e = launch_census2(d_img, nullptr, d_out, nullptr, W, H, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "census");
+    return SGMGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,300 @@
+"""Python binding of the GB300 SGM engine's C ABI (include/sgmgb.h).
+
+Host-side mirror of the reference's plugin interface for Python callers:
+`Engine.run_frame(left, right)` is the single-frame call (common/sgm.h:29-31
+`sgm_run_fn`: host buffers in, disparity map out, 0 or an error), and
+`Plugin` calls the exported `SGM_IMPL` of a built plugin library exactly as
+common/harness.c:150-158 does. Device buffers and streams may come from
+PyTorch (any object with data_ptr(), or a raw integer address).
+
+The compiled library is required: importing this module without it raises,
+and there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD, "libsgmgb.so")
+
+PLAIN, MULTISCALE = 0, 1
+OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_NODEV, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE = 0, -1, -2, -3, -4, -5, -6, -7
+
+# every symbol include/sgmgb.h declares
+EXPORTS = [
+    "sgmgb_abi_version", "sgmgb_strerror", "sgmgb_last_error", "sgmgb_check_desc", "sgmgb_out_size",
+    "sgmgb_workspace_bytes", "sgmgb_create", "sgmgb_destroy", "sgmgb_plan", "sgmgb_run_frame",
+    "sgmgb_run_frame_async", "sgmgb_sync", "sgmgb_census_async", "sgmgb_batch_create", "sgmgb_batch_run",
+    "sgmgb_batch_tile_shape", "sgmgb_batch_destroy", "sgmgb_tune_lookup", "sgmgb_tune_record",
+    "sgmgb_server_create", "sgmgb_server_add_camera", "sgmgb_server_submit", "sgmgb_server_poll",
+    "sgmgb_server_wait", "sgmgb_server_stats_get", "sgmgb_server_destroy", "sgmgb_synth_pair",
+]
+
+
+class FrameDesc(ctypes.Structure):
+    _fields_ = [("W", ctypes.c_int), ("H", ctypes.c_int), ("D", ctypes.c_int),
+                ("paths", ctypes.c_int), ("variant", ctypes.c_int)]
+
+
+class StageTimes(ctypes.Structure):
+    _fields_ = [("census_ms", ctypes.c_double), ("cost_ms", ctypes.c_double),
+                ("aggregate_ms", ctypes.c_double), ("argmin_ms", ctypes.c_double),
+                ("transfer_ms", ctypes.c_double), ("threads_used", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int),
+                ("streams", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("frames_done", ctypes.c_uint64), ("frames_refused", ctypes.c_uint64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("fps", ctypes.c_double), ("resident_bytes", ctypes.c_size_t)]
+
+
+class SgmError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__("%s (%d)%s" % (strerror(code), code, (": " + msg) if msg else ""))
+        self.code = code
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libsgmgb.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, i, u8p, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t
+    fdp = ctypes.POINTER(FrameDesc)
+    sig = {
+        "sgmgb_abi_version": (i, []),
+        "sgmgb_strerror": (ctypes.c_char_p, [i]),
+        "sgmgb_last_error": (ctypes.c_char_p, [vp]),
+        "sgmgb_check_desc": (i, [fdp]),
+        "sgmgb_out_size": (i, [fdp, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "sgmgb_workspace_bytes": (i, [fdp, ctypes.POINTER(sz)]),
+        "sgmgb_create": (i, [i, ctypes.POINTER(vp)]),
+        "sgmgb_destroy": (None, [vp]),
+        "sgmgb_plan": (i, [vp, fdp]),
+        "sgmgb_run_frame": (i, [vp, u8p, u8p, u8p, ctypes.POINTER(StageTimes)]),
+        "sgmgb_run_frame_async": (i, [vp, u8p, u8p, u8p, vp]),
+        "sgmgb_sync": (i, [vp, vp]),
+        "sgmgb_census_async": (i, [vp, u8p, vp, i, i, vp]),
+        "sgmgb_batch_create": (i, [vp, fdp, i, ctypes.POINTER(vp)]),
+        "sgmgb_batch_run": (i, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), vp]),
+        "sgmgb_batch_tile_shape": (i, [vp, i, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "sgmgb_batch_destroy": (None, [vp]),
+        "sgmgb_tune_lookup": (i, [ctypes.c_char_p, fdp, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "sgmgb_tune_record": (i, [ctypes.c_char_p, fdp, i, i, ctypes.c_double]),
+        "sgmgb_server_create": (i, [vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]),
+        "sgmgb_server_add_camera": (i, [vp, i, fdp]),
+        "sgmgb_server_submit": (i, [vp, i, u8p, u8p, ctypes.POINTER(ctypes.c_uint64)]),
+        "sgmgb_server_poll": (i, [vp, ctypes.c_uint64, u8p, ctypes.POINTER(ctypes.c_double)]),
+        "sgmgb_server_wait": (i, [vp, ctypes.c_uint64, u8p, ctypes.POINTER(ctypes.c_double), i]),
+        "sgmgb_server_stats_get": (i, [vp, ctypes.POINTER(ServerStats)]),
+        "sgmgb_server_destroy": (None, [vp]),
+        "sgmgb_synth_pair": (i, [i, i, i, ctypes.c_uint64, u8p, u8p, u8p]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def strerror(code):
+    return lib.sgmgb_strerror(code).decode()
+
+
+def _ptr(x):
+    """Address of a numpy array, a torch tensor, or an integer address."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError("cannot take the address of %r" % type(x))
+
+
+def _stream(s):
+    """cudaStream_t for a torch stream or a raw handle. None selects the
+    engine context's own stream; a handle of 0 (torch's default stream) is
+    passed as cudaStreamLegacy (1) so the engine orders with it."""
+    if s is None:
+        return None
+    h = s if isinstance(s, int) else getattr(s, "cuda_stream", None)
+    if h is None:
+        raise TypeError("not a CUDA stream: %r" % (s,))
+    return h if h != 0 else 1
+
+
+def desc(W, H, D=64, paths=4, variant=PLAIN):
+    return FrameDesc(W, H, D, paths, variant)
+
+
+def check_desc(W, H, D=64, paths=4, variant=PLAIN):
+    return lib.sgmgb_check_desc(ctypes.byref(desc(W, H, D, paths, variant)))
+
+
+def out_size(W, H, D=64, paths=4, variant=PLAIN):
+    w, h = ctypes.c_int(), ctypes.c_int()
+    rc = lib.sgmgb_out_size(ctypes.byref(desc(W, H, D, paths, variant)), ctypes.byref(w), ctypes.byref(h))
+    if rc:
+        raise SgmError(rc)
+    return w.value, h.value
+
+
+def workspace_bytes(W, H, D=64, paths=4, variant=PLAIN):
+    b = ctypes.c_size_t()
+    rc = lib.sgmgb_workspace_bytes(ctypes.byref(desc(W, H, D, paths, variant)), ctypes.byref(b))
+    if rc:
+        raise SgmError(rc)
+    return b.value
+
+
+def synth_pair(W, H, D=64, seed=1):
+    """Seeded synthetic pair (left, right, ground truth) as uint8 arrays of shape (H, W)."""
+    left = np.empty((H, W), np.uint8)
+    right = np.empty((H, W), np.uint8)
+    gt = np.empty((H, W), np.uint8)
+    rc = lib.sgmgb_synth_pair(W, H, D, seed, left.ctypes.data, right.ctypes.data, gt.ctypes.data)
+    if rc:
+        raise SgmError(rc)
+    return left, right, gt
+
+
+class Engine:
+    """One engine context bound to one CUDA device."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        rc = lib.sgmgb_create(device, ctypes.byref(h))
+        if rc:
+            raise SgmError(rc)
+        self.h = h
+        self.fd = None
+
+    def close(self):
+        if self.h:
+            lib.sgmgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc:
+            raise SgmError(rc, lib.sgmgb_last_error(self.h).decode())
+
+    def plan(self, W, H, D=64, paths=4, variant=PLAIN):
+        self.fd = desc(W, H, D, paths, variant)
+        self._check(lib.sgmgb_plan(self.h, ctypes.byref(self.fd)))
+        return self
+
+    def run_frame(self, left, right, times=False):
+        """Host arrays in, host disparity map out (the drop-in call)."""
+        left = np.ascontiguousarray(left, np.uint8)
+        right = np.ascontiguousarray(right, np.uint8)
+        H, W = left.shape
+        if self.fd is None or (self.fd.W, self.fd.H) != (W, H):
+            raise SgmError(ERR_STATE, "plan() this size first")
+        ow, oh = out_size(W, H, self.fd.D, self.fd.paths, self.fd.variant)
+        disp = np.empty((oh, ow), np.uint8)
+        st = StageTimes()
+        self._check(lib.sgmgb_run_frame(self.h, left.ctypes.data, right.ctypes.data, disp.ctypes.data,
+                                        ctypes.byref(st)))
+        return (disp, st.as_dict()) if times else disp
+
+    def run_frame_async(self, d_left, d_right, d_disp, stream=None):
+        """Device buffers (torch tensors or addresses), enqueued on `stream`."""
+        self._check(lib.sgmgb_run_frame_async(self.h, _ptr(d_left), _ptr(d_right), _ptr(d_disp),
+                                              _stream(stream)))
+
+    def sync(self, stream=None):
+        self._check(lib.sgmgb_sync(self.h, _stream(stream)))
+
+    def census_async(self, d_img, d_out, W, H, stream=None):
+        self._check(lib.sgmgb_census_async(self.h, _ptr(d_img), _ptr(d_out), W, H, _stream(stream)))
+
+
+class Batch:
+    """Many frames of mixed shapes planned once and run as one persistent launch."""
+
+    def __init__(self, engine, descs):
+        self.engine = engine
+        self.n = len(descs)
+        arr = (FrameDesc * self.n)(*descs)
+        h = ctypes.c_void_p()
+        engine._check(lib.sgmgb_batch_create(engine.h, arr, self.n, ctypes.byref(h)))
+        self.h = h
+
+    def run(self, d_lefts, d_rights, d_disps, stream=None):
+        A = ctypes.c_void_p * self.n
+        rc = lib.sgmgb_batch_run(self.h, A(*[_ptr(x) for x in d_lefts]), A(*[_ptr(x) for x in d_rights]),
+                                 A(*[_ptr(x) for x in d_disps]), _stream(stream))
+        self.engine._check(rc)
+
+    def tile_shape(self, i):
+        w, l = ctypes.c_int(), ctypes.c_int()
+        self.engine._check(lib.sgmgb_batch_tile_shape(self.h, i, ctypes.byref(w), ctypes.byref(l)))
+        return w.value, l.value
+
+    def close(self):
+        if self.h:
+            lib.sgmgb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plugin:
+    """A built sgm.h plugin library; calls its SGM_IMPL.run like the reference harness."""
+
+    RUN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                           ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(StageTimes))
+
+    class Impl(ctypes.Structure):
+        pass
+
+    Impl._fields_ = [("name", ctypes.c_char_p), ("run", RUN)]
+
+    def __init__(self, D=64, paths=4):
+        path = os.path.join(BUILD, "libsgm_gb300_d%d_p%d.so" % (D, paths))
+        if not os.path.exists(path):
+            raise ImportError("plugin library %s is not built" % path)
+        self.lib = ctypes.CDLL(path)
+        self.impl = Plugin.Impl.in_dll(self.lib, "SGM_IMPL")
+        self.name = self.impl.name.decode()
+
+    def run(self, left, right, threads=0):
+        left = np.ascontiguousarray(left, np.uint8)
+        right = np.ascontiguousarray(right, np.uint8)
+        H, W = left.shape
+        disp = np.zeros((H, W), np.uint8)
+        st = StageTimes(-1, -1, -1, -1, -1, 0)
+        rc = self.impl.run(left.ctypes.data, right.ctypes.data, W, H, disp.ctypes.data, threads,
+                           ctypes.byref(st))
+        return rc, disp, st.as_dict()

@@ -1,0 +1,171 @@
+"""Bit-exact parity of the CUDA engine with the oracle (common/sgm_ref.c,
+multiscale/sgm_ms_ref.c restated in oracle/sgm_oracle.c), through the C ABI.
+
+Integer work: every comparison is byte-for-byte (tolerance 0)."""
+import numpy as np
+import pytest
+
+import oracle
+import sgmgb
+
+pytestmark = pytest.mark.gpu
+
+
+def _rand(H, W, seed):
+    return np.random.default_rng(seed).integers(0, 256, size=(H, W), dtype=np.uint8)
+
+
+def _first_diff(got, want):
+    idx = np.argwhere(got != want)
+    if not len(idx):
+        return ""
+    y, x = idx[0][:2]
+    return " first diff at (x=%d,y=%d): got %d want %d; %d differ" % (x, y, got[y, x], want[y, x], len(idx))
+
+
+# ---- census descriptors (test pattern of common/test_phase1.c:17-62) ----
+@pytest.mark.parametrize("W,H", [(1, 1), (5, 3), (9, 7), (33, 10), (640, 480), (1001, 37)])
+def test_census_descriptors(engine, W, H):
+    import torch
+    for img in (_rand(H, W, W * H), sgmgb.synth_pair(max(W, 2), max(H, 2), 64, 3)[0][:H, :W]):
+        img = np.ascontiguousarray(img)
+        d_img = torch.from_numpy(img).cuda()
+        d_out = torch.empty((H, W), dtype=torch.int64, device="cuda")
+        engine.census_async(d_img, d_out, W, H)
+        engine.sync()
+        torch.cuda.synchronize()
+        got = d_out.cpu().numpy().view(np.uint64)
+        want = oracle.census(img)
+        if not np.array_equal(got, want):
+            y, x = np.argwhere(got != want)[0]
+            xor = int(got[y, x]) ^ int(want[y, x])
+            pytest.fail("census diff at (%d,%d): got %016x want %016x lowest bit %d"
+                        % (x, y, int(got[y, x]), int(want[y, x]), (xor & -xor).bit_length() - 1))
+
+
+# ---- plain SGM: edge cases, disparity ranges, path counts ----
+@pytest.mark.parametrize("W,H", [(1, 1), (1, 23), (23, 1), (2, 2), (15, 9), (40, 9), (63, 31),
+                                 (64, 64), (97, 45), (130, 3)])
+@pytest.mark.parametrize("D,paths", [(16, 4), (64, 4), (64, 8), (128, 8)])
+def test_plain_small(engine, W, H, D, paths):
+    left, right = _rand(H, W, 1), _rand(H, W, 2)
+    engine.plan(W, H, D, paths)
+    got = engine.run_frame(left, right)
+    want = oracle.plain(left, right, D, paths)
+    assert np.array_equal(got, want), _first_diff(got, want)
+
+
+@pytest.mark.parametrize("D", [16, 32, 48, 64, 80, 96, 112, 128, 144, 176, 192, 208, 240, 256])
+def test_plain_disparity_ranges(engine, D):
+    W, H = 300, 70
+    left, right, _ = sgmgb.synth_pair(W, H, min(D, 200), seed=D)
+    for paths in (4, 8):
+        engine.plan(W, H, D, paths)
+        got = engine.run_frame(left, right)
+        want = oracle.plain(left, right, D, paths)
+        assert np.array_equal(got, want), ("D=%d paths=%d" % (D, paths)) + _first_diff(got, want)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_plain_640x480_d64(engine, seed):
+    """The reference's CPU-runnable configuration: 640x480, D=64, 4 paths."""
+    left, right, _ = sgmgb.synth_pair(640, 480, 64, seed)
+    engine.plan(640, 480, 64, 4)
+    got = engine.run_frame(left, right)
+    want = oracle.plain(left, right, 64, 4)
+    assert np.array_equal(got, want), _first_diff(got, want)
+
+
+def test_plain_ties_and_flat(engine):
+    """Flat and periodic images make many tied minima: the lowest d must win."""
+    W, H = 200, 60
+    flat = np.full((H, W), 128, np.uint8)
+    stripes = np.tile((np.arange(W) % 7 * 30).astype(np.uint8), (H, 1))
+    for l, r in ((flat, flat), (stripes, stripes), (stripes, np.roll(stripes, 3, axis=1))):
+        for D, paths in ((64, 4), (64, 8), (128, 4)):
+            engine.plan(W, H, D, paths)
+            got = engine.run_frame(l, r)
+            want = oracle.plain(l, r, D, paths)
+            assert np.array_equal(got, want), _first_diff(got, want)
+
+
+# ---- multi-scale ----
+@pytest.mark.parametrize("W,H", [(2, 2), (4, 6), (16, 10), (64, 48), (130, 66), (320, 200)])
+def test_multiscale_small(engine, W, H):
+    left, right = _rand(H, W, 11), _rand(H, W, 12)
+    engine.plan(W, H, 64, 8, sgmgb.MULTISCALE)
+    got = engine.run_frame(left, right)
+    want = oracle.multiscale(left, right)
+    assert np.array_equal(got, want), _first_diff(got, want)
+
+
+def test_multiscale_synthetic(engine):
+    left, right, _ = sgmgb.synth_pair(480, 320, 64, 5)
+    engine.plan(480, 320, 64, 8, sgmgb.MULTISCALE)
+    got = engine.run_frame(left, right)
+    assert np.array_equal(got, oracle.multiscale(left, right))
+
+
+def test_rejects_bad_descriptions(engine):
+    for args in ((0, 10, 64, 4, 0), (10, 10, 65, 4, 0), (10, 10, 272, 4, 0), (10, 10, 64, 6, 0),
+                 (11, 10, 64, 8, 1), (10, 10, 128, 8, 1), (10, 10, 64, 4, 1)):
+        with pytest.raises(sgmgb.SgmError) as e:
+            engine.plan(*args)
+        assert e.value.code == sgmgb.ERR_ARG
+
+
+# ---- the reference's committed goldens, rebuilt from their generator ----
+@pytest.mark.parametrize("golden", ["data/golden/synthetic.pgm", "data/shared/golden_d64.pgm",
+                                    "data/shared/golden_d128.pgm", "data/shared/golden_d256.pgm",
+                                    "data/multiscale/golden_ms.pgm", "data/multiscale/golden_ms_1080.pgm"])
+def test_reference_goldens(engine, ref_fixtures, golden):
+    g = ref_fixtures["goldens"][golden]
+    s = ref_fixtures["scenes"][g["scene"]]
+    left, right, _ = oracle.gen_reference(s["W"], s["H"], s["gen_D"], s["seed"])
+    import hashlib
+    assert hashlib.sha256(left.tobytes()).hexdigest() == s["sha256_left"]
+    assert hashlib.sha256(right.tobytes()).hexdigest() == s["sha256_right"]
+    variant = sgmgb.PLAIN if g["variant"] == "plain" else sgmgb.MULTISCALE
+    engine.plan(s["W"], s["H"], g["D"], g["paths"], variant)
+    got = engine.run_frame(left, right)
+    assert got.shape == (g["H"], g["W"])
+    assert oracle.fnv1a64(got) == g["fnv1a64"], "%s: FNV mismatch" % golden
+
+
+# ---- the sgm.h plugin (SGM_IMPL) exactly as the reference harness calls it ----
+@pytest.mark.parametrize("D,paths", [(64, 4), (128, 4), (64, 8)])
+def test_plugin_sgm_impl(D, paths):
+    plug = sgmgb.Plugin(D, paths)
+    assert plug.name == "gb300"
+    left, right, _ = sgmgb.synth_pair(320, 240, D, 9)
+    for _ in range(2):   # second call reuses the resident state
+        rc, disp, st = plug.run(left, right, threads=4)
+        assert rc == 0
+        assert np.array_equal(disp, oracle.plain(left, right, D, paths))
+    assert st["aggregate_ms"] >= 0 and st["census_ms"] >= 0 and st["transfer_ms"] >= 0
+    assert st["cost_ms"] == -1 and st["argmin_ms"] == -1 and st["threads_used"] == 0
+    rc, disp, st = plug.run(left[:100, :150], right[:100, :150])   # resolution change re-plans
+    assert rc == 0 and np.array_equal(disp, oracle.plain(left[:100, :150], right[:100, :150], D, paths))
+
+
+def test_plugin_rejects_empty_frame():
+    plug = sgmgb.Plugin(64, 4)
+    rc, _, _ = plug.run(np.zeros((0, 5), np.uint8), np.zeros((0, 5), np.uint8))
+    assert rc != 0
+
+
+# ---- full size: 1080p D=64 (configuration A) and the async device path ----
+def test_config_a_full_size_async(engine):
+    import torch
+    left, right, _ = sgmgb.synth_pair(1920, 1080, 64, 1)
+    want = oracle.plain(left, right, 64, 4)
+    engine.plan(1920, 1080, 64, 4)
+    dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
+    dd = torch.empty((1080, 1920), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    for _ in range(2):
+        engine.run_frame_async(dl, dr, dd, stream=s)
+    s.synchronize()
+    assert np.array_equal(dd.cpu().numpy(), want)
+    # host path gives the same bytes
+    assert np.array_equal(engine.run_frame(left, right), want)
