@@ -37,7 +37,7 @@ WORKLOAD = "configA_1920x1080_D64_4path"
 METRIC = "MDE/s (W*H*D per second), 1080p D=64 4-path, bit-exact"
 UNIT = "MDE/s"
 B_ALG = 2 * W * H * D + 3 * W * H          # modelled minimal bytes per frame
-KERNELS_PER_FRAME = 1 + PATHS               # census + one pass per direction
+KERNELS_PER_FRAME = 2 + PATHS               # census + cost volume + one pass per direction
 
 
 def peaks():

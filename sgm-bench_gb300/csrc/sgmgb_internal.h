@@ -35,6 +35,8 @@ struct FrameSlot {
     size_t bytes = 0;
     uint8_t *left = nullptr, *right = nullptr, *disp = nullptr;   // inputs / output
     uint64_t *cl = nullptr, *cr = nullptr;                        // full-scale census
+    uint8_t *C = nullptr;                                         // W*H*D cost volume
+    uint8_t *C1 = nullptr;                                        // half-scale cost volume (multi-scale)
     uint8_t *sc = nullptr;                                        // W*H*D scratch L
     uint16_t *S = nullptr;                                        // W*H*D sum
     // multi-scale extras
@@ -43,6 +45,9 @@ struct FrameSlot {
     uint8_t *hsobL = nullptr, *hsobR = nullptr;                   // half-scale SobelX
     uint64_t *cl1 = nullptr, *cr1 = nullptr;                      // half-scale census
     uint8_t *disp1 = nullptr;                                     // stage-1 argmin (defined work, unused)
+    // independent path passes of one frame run on forked streams
+    cudaStream_t aux[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
 };
 
 namespace sgmgb {

@@ -8,43 +8,41 @@
 
 namespace sgmgb {
 
-// How the cost of one (pixel, d) is formed.
-enum CostKind : int {
-    COST_PLAIN = 0,   // popcount(cl ^ cr), invalid 62              (common/sgm_ref.c:44-56)
-    COST_MS1   = 1,   // popcount(cl ^ cr), invalid 63, half scale  (multiscale/sgm_ms_ref.c:66-72)
-    COST_MS2   = 2    // (full + half(x/2,y/2,d/2) + 1) >> 1         (multiscale/sgm_ms_ref.c:184-188)
-};
+// Invalid-disparity cost (x - d < 0) of each variant: 62 in the plain method
+// (common/sgm_params.h:27-29), 63 in the multi-scale one (multiscale/sgm_ms_ref.c:41).
+constexpr int kInvalidPlain = 62, kInvalidMultiscale = 63;
 
-// What a path pass does with its L(p,d) at every pixel it visits. Directions
-// are run in opposite-direction pairs: the first of a pair parks its L in a
-// uint8 scratch plane, the second adds both into the uint16 sum S.
+// What a path pass does with its L(p,d) at every pixel it visits.
 enum PassMode : int {
     MODE_SCRATCH = 0,   // sc = L
     MODE_STORE   = 1,   // S  = sc + L           (first pair: no memset of S)
     MODE_ACCUM   = 2,   // S += sc + L
-    MODE_FINAL   = 3    // argmin_d(S + sc + L) -> disp, lowest d on ties
+    MODE_FINAL   = 3,   // argmin_d(S + sc + L) -> disp, lowest d on ties
+    MODE_FINAL3  = 4    // argmin_d(sc + sc2 + sc3 + L) -> disp: three other directions' planes
 };
 
 struct LineParams {
-    const uint64_t *cl, *cr;     // census descriptors at this scale, W*H
-    const uint64_t *cl1, *cr1;   // half-scale descriptors (COST_MS2 only), (W/2)*(H/2)
-    uint8_t  *sc;                // W*H*D scratch L
+    const uint8_t *C;            // cost volume at this scale, W*H*D
+    uint8_t  *sc;                // W*H*D scratch L (written by SCRATCH, read otherwise)
+    const uint8_t *sc2, *sc3;    // MODE_FINAL3: the second and third planes
     uint16_t *S;                 // W*H*D sum
-    uint8_t  *disp;              // MODE_FINAL output
+    uint8_t  *disp;              // final passes' output
     int W, H, D;
-    int nl;                      // active lanes: D / DPL
+    int nl;                      // lanes of a line that hold disparities: D / DPL (set by launch_line)
+    int lpl, gpw;                // lanes per line, lines per warp (set by launch_line)
     int dx, dy;                  // direction of travel
     int p1, p2;                  // penalties
     int nlines;                  // independent lines for this direction
-    int even_only;               // MODE_FINAL: argmin only at even (x,y) into a (W/2)x(H/2) map
+    int even_only;               // final: argmin only at even (x,y) into a (W/2)x(H/2) map
+    int key16;                   // final: S*64 + d fits 16 bits (4 paths, D <= 64)
 };
 
-// Disparities per lane for a disparity range: the smallest even count that
-// divides D and needs at most 32 lanes.
+// Disparities per lane: 2 up to D = 64, 4 up to 128, 8 up to 256; D/DPL lanes
+// per line and 32/(D/DPL) lines per warp when that divides 32. Few
+// disparities per lane keep many warps per direction.
 inline int dpl_for(int D) {
-    for (int dpl = 2; dpl <= 8; dpl += 2)
-        if (D % dpl == 0 && D / dpl <= 32) return dpl;
-    return 0;
+    if (D < 16 || D > 256 || D % 16) return 0;
+    return D <= 64 ? 2 : (D <= 128 ? 4 : 8);
 }
 
 // Number of independent lines a direction decomposes the image into.
@@ -61,7 +59,12 @@ cudaError_t launch_sobel2(const uint8_t *im0, const uint8_t *im1, uint8_t *out0,
                           int W, int H, cudaStream_t s);
 cudaError_t launch_half2(const uint8_t *im0, const uint8_t *im1, uint8_t *out0, uint8_t *out1,
                          int W, int H, cudaStream_t s);
-cudaError_t launch_line(const LineParams &p, int mode, int cost_kind, int saturate,
-                        int warps_per_block, cudaStream_t s);
+// Cost volume (uint8, W*H*D) from census descriptors; C1 != NULL makes the
+// multi-scale full-scale cost averaged with the half-scale volume C1.
+cudaError_t launch_cost(const uint64_t *cl, const uint64_t *cr, uint8_t *C, const uint8_t *C1,
+                        int W, int H, int D, int invalid, cudaStream_t s);
+// One direction's path pass over the cost volume p.C (sgmgb_path.cu).
+// saturate: clamp L to 255 (multi-scale). warps_per_block in 1..4.
+cudaError_t launch_line(const LineParams &p, int mode, int saturate, int warps_per_block, cudaStream_t s);
 
 }  // namespace sgmgb

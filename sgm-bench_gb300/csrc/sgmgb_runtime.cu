@@ -25,21 +25,24 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
     const size_t out_n = fd.variant == SGMGB_MULTISCALE ? (W / 2) * (H / 2) : N;
     const size_t o_disp = take(out_n);
     const size_t o_cl = take(N * 8), o_cr = take(N * 8);
-    const size_t o_sc = take(N * D), o_S = take(N * D * 2);
+    const size_t o_C = take(N * D), o_sc = take(N * D), o_S = take(N * D * 2);
     size_t o_sobL = 0, o_sobR = 0, o_hL = 0, o_hR = 0, o_hsL = 0, o_hsR = 0, o_cl1 = 0, o_cr1 = 0, o_d1 = 0;
+    size_t o_C1 = 0;
     if (fd.variant == SGMGB_MULTISCALE) {
         const size_t Nh = (W / 2) * (H / 2);
         o_sobL = take(N); o_sobR = take(N);
         o_hL = take(Nh); o_hR = take(Nh); o_hsL = take(Nh); o_hsR = take(Nh);
         o_cl1 = take(Nh * 8); o_cr1 = take(Nh * 8);
         o_d1 = take(Nh);
+        o_C1 = take(Nh * D);
     }
     if (s) {
         uint8_t *b = (uint8_t *)s->base;
         s->left = b + o_left; s->right = b + o_right; s->disp = b + o_disp;
         s->cl = (uint64_t *)(b + o_cl); s->cr = (uint64_t *)(b + o_cr);
-        s->sc = b + o_sc; s->S = (uint16_t *)(b + o_S);
+        s->C = b + o_C; s->sc = b + o_sc; s->S = (uint16_t *)(b + o_S);
         if (fd.variant == SGMGB_MULTISCALE) {
+            s->C1 = b + o_C1;
             s->sobL = b + o_sobL; s->sobR = b + o_sobR;
             s->halfL = b + o_hL; s->halfR = b + o_hR; s->hsobL = b + o_hsL; s->hsobR = b + o_hsR;
             s->cl1 = (uint64_t *)(b + o_cl1); s->cr1 = (uint64_t *)(b + o_cr1);
@@ -62,12 +65,24 @@ int slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err) {
         return SGMGB_ERR_NOMEM;
     }
     slot_layout(fd, s);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaStreamCreateWithFlags(&s->aux[i], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->join[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        err = std::string("stream/event creation: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        slot_free(s);
+        return SGMGB_ERR_CUDA;
+    }
     *out = s;
     return SGMGB_OK;
 }
 
 void slot_free(FrameSlot *s) {
     if (!s) return;
+    for (auto &a : s->aux) if (a) cudaStreamDestroy(a);
+    if (s->fork) cudaEventDestroy(s->fork);
+    for (auto &j : s->join) if (j) cudaEventDestroy(j);
     if (s->base) cudaFree(s->base);
     delete s;
 }
@@ -86,15 +101,15 @@ static const PassSpec kPasses8[8] = {
 
 static int ms_p1(int dx, int dy) { return dy == 0 ? 40 : (dx == 0 ? 20 : 10); }
 
-static cudaError_t run_paths(const LineParams &base, int paths, int cost_kind, int sat, bool ms,
-                             int wpb, cudaStream_t st) {
+static cudaError_t run_paths(const LineParams &base, int paths, int sat, bool ms, int wpb,
+                             cudaStream_t st) {
     const PassSpec *ps = paths == 8 ? kPasses8 : kPasses4;
     for (int i = 0; i < paths; i++) {
         LineParams p = base;
         p.dx = ps[i].dx; p.dy = ps[i].dy;
         p.p1 = ms ? ms_p1(p.dx, p.dy) : 20;
         p.nlines = lines_for(p.W, p.H, p.dx, p.dy);
-        cudaError_t e = launch_line(p, ps[i].mode, cost_kind, sat, wpb, st);
+        cudaError_t e = launch_line(p, ps[i].mode, sat, wpb, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -107,31 +122,64 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
     cudaError_t e;
     if (fd.variant == SGMGB_PLAIN) {
         if ((e = launch_census2(d_left, d_right, s.cl, s.cr, fd.W, fd.H, st)) != cudaSuccess) return e;
+        if ((e = launch_cost(s.cl, s.cr, s.C, nullptr, fd.W, fd.H, fd.D, kInvalidPlain, st)) != cudaSuccess)
+            return e;
         if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
         LineParams p{};
-        p.cl = s.cl; p.cr = s.cr; p.sc = s.sc; p.S = s.S; p.disp = d_disp;
+        p.C = s.C; p.sc = s.sc; p.S = s.S; p.disp = d_disp;
         p.W = fd.W; p.H = fd.H; p.D = fd.D; p.nl = fd.D / dpl_for(fd.D);
-        p.p2 = 192; p.even_only = 0;
-        if ((e = run_paths(p, fd.paths, COST_PLAIN, 0, false, wpb, st)) != cudaSuccess) return e;
+        p.p2 = 192; p.even_only = 0; p.p1 = 20;
+        p.key16 = (fd.paths == 4 && fd.D <= 64) ? 1 : 0;
+        if (fd.paths == 8) {
+            if ((e = run_paths(p, fd.paths, 0, false, wpb, st)) != cudaSuccess) return e;
+        } else {
+            // 4 paths: R->L, B->T and L->R are independent; each parks its L in
+            // a uint8 plane (the sum buffer's bytes hold planes 2 and 3) on its
+            // own stream, then T->B adds all four and takes the argmin.
+            const size_t plane = (size_t)fd.W * fd.H * fd.D;
+            uint8_t *pl[3] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane};
+            const int dir[3][2] = {{-1, 0}, {0, -1}, {1, 0}};
+            cudaStream_t ss[3] = {st, s.aux[0], s.aux[1]};
+            if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
+            for (int k = 1; k < 3; k++)
+                if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
+            for (int k = 0; k < 3; k++) {
+                LineParams q = p;
+                q.dx = dir[k][0]; q.dy = dir[k][1]; q.sc = pl[k];
+                q.nlines = lines_for(q.W, q.H, q.dx, q.dy);
+                if ((e = launch_line(q, MODE_SCRATCH, 0, wpb, ss[k])) != cudaSuccess) return e;
+            }
+            for (int k = 1; k < 3; k++) {
+                if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
+                if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
+            }
+            LineParams q = p;
+            q.dx = 0; q.dy = 1; q.sc = pl[0]; q.sc2 = pl[1]; q.sc3 = pl[2];
+            q.nlines = lines_for(q.W, q.H, 0, 1);
+            if ((e = launch_line(q, MODE_FINAL3, 0, wpb, st)) != cudaSuccess) return e;
+        }
     } else {
         const int W = fd.W, H = fd.H, hw = W / 2, hh = H / 2;
         // stage 1: half scale (multiscale/sgm_ms_ref.c:168-181)
         if ((e = launch_half2(d_left, d_right, s.halfL, s.halfR, W, H, st)) != cudaSuccess) return e;
         if ((e = launch_sobel2(s.halfL, s.halfR, s.hsobL, s.hsobR, hw, hh, st)) != cudaSuccess) return e;
         if ((e = launch_census2(s.hsobL, s.hsobR, s.cl1, s.cr1, hw, hh, st)) != cudaSuccess) return e;
+        if ((e = launch_cost(s.cl1, s.cr1, s.C1, nullptr, hw, hh, 64, kInvalidMultiscale, st)) != cudaSuccess)
+            return e;
         if ((e = launch_sobel2(d_left, d_right, s.sobL, s.sobR, W, H, st)) != cudaSuccess) return e;
         if ((e = launch_census2(s.sobL, s.sobR, s.cl, s.cr, W, H, st)) != cudaSuccess) return e;
+        if ((e = launch_cost(s.cl, s.cr, s.C, s.C1, W, H, 64, kInvalidMultiscale, st)) != cudaSuccess)
+            return e;
         if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
         LineParams p1{};
-        p1.cl = s.cl1; p1.cr = s.cr1; p1.sc = s.sc; p1.S = s.S; p1.disp = s.disp1;
+        p1.C = s.C1; p1.sc = s.sc; p1.S = s.S; p1.disp = s.disp1;
         p1.W = hw; p1.H = hh; p1.D = 64; p1.nl = 32; p1.p2 = 200; p1.even_only = 0;
-        if ((e = run_paths(p1, 8, COST_MS1, 1, true, wpb, st)) != cudaSuccess) return e;
+        if ((e = run_paths(p1, 8, 1, true, wpb, st)) != cudaSuccess) return e;
         // stage 2: full scale, cost averaged with the half-scale cost (:183-199)
         LineParams p2{};
-        p2.cl = s.cl; p2.cr = s.cr; p2.cl1 = s.cl1; p2.cr1 = s.cr1; p2.sc = s.sc; p2.S = s.S;
-        p2.disp = d_disp;
+        p2.C = s.C; p2.sc = s.sc; p2.S = s.S; p2.disp = d_disp;
         p2.W = W; p2.H = H; p2.D = 64; p2.nl = 32; p2.p2 = 200; p2.even_only = 1;
-        if ((e = run_paths(p2, 8, COST_MS2, 1, true, wpb, st)) != cudaSuccess) return e;
+        if ((e = run_paths(p2, 8, 1, true, wpb, st)) != cudaSuccess) return e;
     }
     if (ev_end && (e = cudaEventRecord(ev_end, st)) != cudaSuccess) return e;
     return cudaSuccess;
