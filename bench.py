@@ -196,6 +196,7 @@ def run_gb300(args):
     dev = torch.device("cuda", local)
     eng = sgmgb.Engine(local)
     eng.plan(W, H, D, PATHS)
+    eng.set_path_shape(args.warps_per_block, args.disp_per_lane)
     # 8 distinct resident pairs, round-robin: inputs differ every step and the
     # per-frame working set (about 430 MB of census, scratch and sum planes)
     # is far larger than the 129 MB L2.
@@ -310,6 +311,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--warps-per-block", type=int, default=4, help="path-kernel shape (speed only)")
+    ap.add_argument("--disp-per-lane", type=int, default=0, help="path-kernel shape: 0, 2, 4 or 8")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

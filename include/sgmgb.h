@@ -85,6 +85,11 @@ int  sgmgb_create(int device, sgmgb_ctx **out);
 void sgmgb_destroy(sgmgb_ctx *ctx);
 /* Sizes the context's resident single-frame workspace (re-plans on change). */
 int  sgmgb_plan(sgmgb_ctx *ctx, const sgmgb_frame_desc *fd);
+/* Path-kernel shape of the context's frames: warps per block (1..4) and
+ * disparities per lane (0, 2, 4 or 8, raised to the smallest value that fits
+ * a line in one warp: 2 up to D = 64, 4 up to 128, 8 up to 256). Results do
+ * not depend on it, only speed. Drops cached graphs. */
+int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane);
 
 /* ---- single frame ---- */
 /* Host buffers in and out, synchronous: the drop-in call. left/right are
@@ -114,18 +119,19 @@ int  sgmgb_batch_create(sgmgb_ctx *ctx, const sgmgb_frame_desc *frames, int n,
  * arrays of device pointers). Enqueued on `stream`; returns without waiting. */
 int  sgmgb_batch_run(sgmgb_batch *b, const uint8_t *const *d_left,
                      const uint8_t *const *d_right, uint8_t *const *d_disp, void *stream);
-/* Tile shape chosen for frame i: warps per block and lines per tile. */
+/* Path-kernel shape chosen for frame i: warps per block and disparities per lane. */
 int  sgmgb_batch_tile_shape(const sgmgb_batch *b, int i, int *warps_per_block,
-                            int *lines_per_tile);
+                            int *disp_per_lane);
 void sgmgb_batch_destroy(sgmgb_batch *b);
 
 /* ---- autotuner cache (host-only; no GPU needed) ---- */
-/* Records / looks up the chosen tile shape for a frame shape. The cache file
- * is a plain text table "W H D paths variant warps lines us". */
+/* Records / looks up the chosen path-kernel shape for a frame shape. The
+ * cache file is a plain text table "W H D paths variant warps dpl us"; the
+ * last matching line wins. */
 int sgmgb_tune_lookup(const char *cache_path, const sgmgb_frame_desc *fd,
-                      int *warps_per_block, int *lines_per_tile);
+                      int *warps_per_block, int *disp_per_lane);
 int sgmgb_tune_record(const char *cache_path, const sgmgb_frame_desc *fd,
-                      int warps_per_block, int lines_per_tile, double us);
+                      int warps_per_block, int disp_per_lane, double us);
 
 /* ---- server: continuous batching of camera frames ---- */
 typedef struct sgmgb_server sgmgb_server;

@@ -7,6 +7,13 @@
 #include "../../include/sgmgb.h"
 #include "sgmgb_kernels.cuh"
 
+// Shape of the path kernels: warps per block and disparities per lane
+// (0 = the smallest valid). Only speed depends on it.
+struct PathShape {
+    int wpb = 4;
+    int dpl = 0;
+};
+
 struct sgmgb_ctx {
     int device = 0;
     int sm_count = 0;
@@ -24,7 +31,7 @@ struct sgmgb_ctx {
     cudaGraphExec_t graph[kGraphs] = {};
     const void *graph_key[kGraphs][3] = {};
     int graph_next = 0;
-    int warps_per_block = 4;
+    PathShape shape;
 };
 
 // Device buffers of one frame slot. All pointers are carved from one
@@ -58,10 +65,10 @@ int  slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err);
 void slot_free(FrameSlot *s);
 
 // Enqueues the whole frame pipeline for `s` reading d_left/d_right and
-// writing d_disp on `st`. Events ev_census / ev_agg (optional) are recorded
-// after the census phase and at the end. warps_per_block: path-kernel shape.
+// writing d_disp on `st`. Events ev_census / ev_end (optional) are recorded
+// after the cost volume and at the end.
 cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8_t *d_right,
-                          uint8_t *d_disp, cudaStream_t st, int warps_per_block,
+                          uint8_t *d_disp, cudaStream_t st, const PathShape &shape,
                           cudaEvent_t ev_census, cudaEvent_t ev_end);
 
 int set_err(sgmgb_ctx *ctx, int code, const std::string &msg);

@@ -35,15 +35,14 @@ struct LineParams {
     int nlines;                  // independent lines for this direction
     int even_only;               // final: argmin only at even (x,y) into a (W/2)x(H/2) map
     int key16;                   // final: S*64 + d fits 16 bits (4 paths, D <= 64)
+    int dpl;                     // disparities per lane: 2, 4 or 8; 0 picks the smallest valid
 };
 
-// Disparities per lane: 2 up to D = 64, 4 up to 128, 8 up to 256; D/DPL lanes
-// per line and 32/(D/DPL) lines per warp when that divides 32. Few
-// disparities per lane keep many warps per direction.
-inline int dpl_for(int D) {
-    if (D < 16 || D > 256 || D % 16) return 0;
-    return D <= 64 ? 2 : (D <= 128 ? 4 : 8);
-}
+// Disparities per lane of the path kernel: `want` (0, 2, 4 or 8) raised to
+// the smallest value that fits a line in one warp (D/DPL <= 32 lanes: 2 up to
+// D = 64, 4 up to 128, 8 up to 256); 0 for an invalid D or want. A line takes
+// D/DPL lanes and a warp 32/(D/DPL) lines when that divides 32.
+int path_dpl(int D, int want);
 
 // Number of independent lines a direction decomposes the image into.
 inline int lines_for(int W, int H, int dx, int dy) {
@@ -63,6 +62,9 @@ cudaError_t launch_half2(const uint8_t *im0, const uint8_t *im1, uint8_t *out0, 
 // multi-scale full-scale cost averaged with the half-scale volume C1.
 cudaError_t launch_cost(const uint64_t *cl, const uint64_t *cr, uint8_t *C, const uint8_t *C1,
                         int W, int H, int D, int invalid, cudaStream_t s);
+// Sets the path kernels' shared-memory limits; call once per device before
+// the first launch (and outside stream capture).
+cudaError_t prepare_path_kernels();
 // One direction's path pass over the cost volume p.C (sgmgb_path.cu).
 // saturate: clamp L to 255 (multi-scale). warps_per_block in 1..4.
 cudaError_t launch_line(const LineParams &p, int mode, int saturate, int warps_per_block, cudaStream_t s);

@@ -21,10 +21,18 @@
 // (v | v << 16), so the result is already the packed pair the next step needs.
 // Lanes past the last disparity carry cost 0x3FFF, so they never win a
 // minimum. The multi-scale variant clamps L to 255 (multiscale/sgm_ms_ref.c:82).
+// The first pixel of a line needs no special case: with L_prev = 0 and
+// min_prev = 0 the recurrence gives L = C, which is the reference's start.
 //
-// Memory: every step's inputs (its cost bytes, the planes of other directions,
-// the partial sum) are loaded R steps ahead into a register ring.
+// Memory: a line's per-step inputs (its cost bytes, the planes of other
+// directions, the partial sum) are streamed into a per-warp shared-memory
+// ring with cp.async, K steps per chunk and NCH chunks per ring, so three
+// chunks are in flight while the lanes consume the fourth. The copies hold no
+// registers, which is what lets a pass keep enough bytes in flight per SM when
+// only a few lines (warps) run on it -- the case of the horizontal passes.
 #include "sgmgb_kernels.cuh"
+#include <climits>
+#include <type_traits>
 
 namespace sgmgb {
 
@@ -32,6 +40,7 @@ namespace {
 
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr uint32_t kPadPk = 0x3FFF3FFFu;   // cost / L of lanes past the last disparity
+constexpr int NCH = 4;                     // ring depth in chunks
 
 __device__ __forceinline__ uint32_t vmin2(uint32_t a, uint32_t b) {
     uint32_t r;
@@ -48,8 +57,30 @@ __device__ __forceinline__ uint32_t hw_at(const uint32_t (&r)[NR], int k) {
     return (r[k % NR] >> (16 * (k / NR))) & 0xFFFFu;
 }
 
+__device__ __forceinline__ void cp_async16(uint32_t dst_smem, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst_smem), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 template <int MODE> struct Planes {   // scratch planes a pass reads
     static constexpr int N = MODE == MODE_SCRATCH ? 0 : (MODE == MODE_FINAL3 ? 3 : 1);
+};
+
+// Ring geometry of a DPL. A step of one "byte stream" (the cost bytes or a
+// plane: D bytes per line) takes SBM = 32*DPL bytes of the ring whatever the
+// group shape, so lane l always reads its DPL bytes at l*DPL; the partial sum
+// S takes two such units. NGB: 16-byte copies per lane per byte stream per chunk.
+template <int DPL> struct Ring {
+    static constexpr int K = DPL == 8 ? 4 : 8;     // steps per chunk
+    static constexpr int SBM = 32 * DPL;
+    static constexpr int NGB = K * SBM / 512;
+};
+template <int DPL, int MODE> struct Slot {
+    static constexpr bool HAS_S = MODE == MODE_ACCUM || MODE == MODE_FINAL;
+    static constexpr int U = 1 + Planes<MODE>::N + (HAS_S ? 2 : 0);   // byte-stream units per step
+    static constexpr int BYTES = Ring<DPL>::K * Ring<DPL>::SBM * U;  // one chunk of a warp
 };
 
 template <int DPL, int MODE>
@@ -66,63 +97,48 @@ __device__ __forceinline__ void load_bytes(const uint8_t *src, uint32_t *w) {
         w[0] = *(const uint16_t *)src;
     } else if (DPL == 4) {
         w[0] = *(const uint32_t *)src;
-    } else if (DPL == 8) {
+    } else {
         const uint2 v = *(const uint2 *)src;
         w[0] = v.x; w[1] = v.y;
-    } else {
+    }
+}
+
+// Reads step k's inputs of this lane from the ring chunk at `chunk`.
+template <int DPL, int MODE>
+__device__ __forceinline__ void ring_read(const uint8_t *chunk, int lane, int k, StepIn<DPL, MODE> &s) {
+    constexpr int K = Ring<DPL>::K, SBM = Ring<DPL>::SBM, SCW = StepIn<DPL, MODE>::SCW;
+    const uint8_t *b = chunk + k * SBM + lane * DPL;
+    load_bytes<DPL>(b, s.cw);
 #pragma unroll
-        for (int k = 0; k < (DPL + 3) / 4; k++) w[k] = 0;
-#pragma unroll
-        for (int k = 0; k < DPL; k++) w[k / 4] |= (uint32_t)src[k] << (8 * (k % 4));
+    for (int q = 0; q < Planes<MODE>::N; q++) load_bytes<DPL>(b + (1 + q) * K * SBM, s.pw + q * SCW);
+    if (Slot<DPL, MODE>::HAS_S) {
+        const uint8_t *sb = chunk + (1 + Planes<MODE>::N) * K * SBM + k * 2 * SBM + lane * 2 * DPL;
+        if (DPL == 2) {
+            s.sw[0] = *(const uint32_t *)sb;
+        } else if (DPL == 4) {
+            const uint2 w = *(const uint2 *)sb;
+            s.sw[0] = w.x; s.sw[1] = w.y;
+        } else {
+            const uint4 w = *(const uint4 *)sb;
+            s.sw[0] = w.x; s.sw[1] = w.y; s.sw[2] = w.z; s.sw[3] = w.w;
+        }
     }
 }
 
 // byte k of a packed byte run
 __device__ __forceinline__ uint32_t byte_at(const uint32_t *w, int k) { return (w[k / 4] >> (8 * (k % 4))) & 0xFFu; }
 
-// Loads everything pixel p's step reads.
-template <int DPL, int MODE>
-__device__ __forceinline__ void fetch(const LineParams &P, int p, int d0, StepIn<DPL, MODE> &s) {
-    constexpr int SCW = StepIn<DPL, MODE>::SCW;
-    const size_t off = (size_t)p * P.D + d0;
-    load_bytes<DPL>(P.C + off, s.cw);
-    if (Planes<MODE>::N > 0) {
-        load_bytes<DPL>(P.sc + off, s.pw);
-        if (MODE == MODE_FINAL3) {
-            load_bytes<DPL>(P.sc2 + off, s.pw + SCW);
-            load_bytes<DPL>(P.sc3 + off, s.pw + 2 * SCW);
-        }
-        if (MODE == MODE_ACCUM || MODE == MODE_FINAL) {
-            const uint32_t *sp = (const uint32_t *)(P.S + off);
-            if (DPL == 4) {
-                const uint2 w = *(const uint2 *)sp;
-                s.sw[0] = w.x; s.sw[1] = w.y;
-            } else if (DPL == 8) {
-                const uint4 w = *(const uint4 *)sp;
-                s.sw[0] = w.x; s.sw[1] = w.y; s.sw[2] = w.z; s.sw[3] = w.w;
-            } else {
-#pragma unroll
-                for (int i = 0; i < DPL / 2; i++) s.sw[i] = sp[i];
-            }
-        }
-    }
-}
-
 // Packed costs, register j = (d0+j, d0+DPL/2+j).
 template <int DPL, int MODE>
 __device__ __forceinline__ void unpack_cost(const StepIn<DPL, MODE> &s, uint32_t (&c)[DPL / 2]) {
-    constexpr int NR = DPL / 2;
     if (DPL == 2) {
         c[0] = __byte_perm(s.cw[0], 0, 0x4140);
     } else if (DPL == 4) {
         c[0] = __byte_perm(s.cw[0], 0, 0x4240);
         c[1] = __byte_perm(s.cw[0], 0, 0x4341);
-    } else if (DPL == 8) {
-#pragma unroll
-        for (int j = 0; j < 4; j++) c[j] = __byte_perm(s.cw[0], s.cw[1], j | ((4 + j) << 8)) & 0x00FF00FFu;
     } else {
 #pragma unroll
-        for (int j = 0; j < NR; j++) c[j] = byte_at(s.cw, j) | (byte_at(s.cw, j + NR) << 16);
+        for (int j = 0; j < 4; j++) c[j] = __byte_perm(s.cw[0], s.cw[1], j | ((4 + j) << 8)) & 0x00FF00FFu;
     }
 }
 // natural-order u16 pair i = (d0+2i, d0+2i+1) of a packed byte run
@@ -132,27 +148,23 @@ __device__ __forceinline__ uint32_t byte_pair(const uint32_t *w, int i) {
 
 // What a pass does with L(p, d0..d0+DPL-1). `live`: this lane's line has a
 // pixel at this step; `lead`: the group's first lane; `gmask`: the group.
-// KEY16: the argmin key S*64 + d fits a packed u16 (4 paths, D <= 64).
+// `out` points at this lane's bytes of pixel p in sc (SCRATCH) or S (STORE,
+// ACCUM). KEY16: the argmin key S*64 + d fits a packed u16 (4 paths, D <= 64).
 template <int DPL, int MODE, bool KEY16>
-__device__ __forceinline__ void emit(const LineParams &P, int p, int x, int y, int d0, bool lead,
-                                     uint32_t gmask, bool live, const uint32_t (&L)[DPL / 2],
+__device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int x, int y, int d0,
+                                     bool lead, uint32_t gmask, bool live, const uint32_t (&L)[DPL / 2],
                                      const StepIn<DPL, MODE> &s) {
     constexpr int NR = DPL / 2;
     constexpr int SCW = StepIn<DPL, MODE>::SCW;
-    const size_t off = (size_t)p * P.D + d0;
     if (MODE == MODE_SCRATCH) {
         if (!live) return;
-        uint8_t *dst = P.sc + off;
         if (DPL == 2) {
-            *(uint16_t *)dst = (uint16_t)__byte_perm(L[0], 0, 0x0020);
+            *(uint16_t *)out = (uint16_t)__byte_perm(L[0], 0, 0x0020);
         } else if (DPL == 4) {
-            *(uint32_t *)dst = __byte_perm(L[0], L[1], 0x6240);
-        } else if (DPL == 8) {
-            const uint32_t t01 = __byte_perm(L[0], L[1], 0x6240), t23 = __byte_perm(L[2], L[3], 0x6240);
-            *(uint2 *)dst = make_uint2(__byte_perm(t01, t23, 0x5410), __byte_perm(t01, t23, 0x7632));
+            *(uint32_t *)out = __byte_perm(L[0], L[1], 0x6240);
         } else {
-#pragma unroll
-            for (int k = 0; k < DPL; k++) dst[k] = (uint8_t)hw_at<NR>(L, k);
+            const uint32_t t01 = __byte_perm(L[0], L[1], 0x6240), t23 = __byte_perm(L[2], L[3], 0x6240);
+            *(uint2 *)out = make_uint2(__byte_perm(t01, t23, 0x5410), __byte_perm(t01, t23, 0x7632));
         }
         return;
     }
@@ -168,17 +180,14 @@ __device__ __forceinline__ void emit(const LineParams &P, int p, int x, int y, i
     }
     if (MODE == MODE_STORE || MODE == MODE_ACCUM) {
         if (!live) return;
-        uint32_t *sp = (uint32_t *)(P.S + off);
-        if (DPL == 4) *(uint2 *)sp = make_uint2(tot[0], tot[1]);
-        else if (DPL == 8) *(uint4 *)sp = make_uint4(tot[0], tot[1], tot[2], tot[3]);
-        else {
-#pragma unroll
-            for (int i = 0; i < NR; i++) sp[i] = tot[i];
-        }
+        uint32_t *sp = (uint32_t *)out;
+        if (DPL == 2) *sp = tot[0];
+        else if (DPL == 4) *(uint2 *)sp = make_uint2(tot[0], tot[1]);
+        else *(uint4 *)sp = make_uint4(tot[0], tot[1], tot[2], tot[3]);
         return;
     }
     // final passes: argmin over d, the lowest d winning ties
-    if (P.even_only && ((x | y) & 1)) return;   // uniform within the group
+    if (MODE == MODE_FINAL && P.even_only && ((x | y) & 1)) return;   // uniform within the group
     uint32_t key;
     if (KEY16) {
         uint32_t k = kFull;
@@ -198,7 +207,7 @@ __device__ __forceinline__ void emit(const LineParams &P, int p, int x, int y, i
     key = __reduce_min_sync(gmask, key);
     if (lead && live) {
         const uint8_t d = (uint8_t)(KEY16 ? (key & 0x3Fu) : (key & 0xFFu));
-        if (P.even_only) P.disp[(size_t)(y >> 1) * (P.W >> 1) + (x >> 1)] = d;
+        if (MODE == MODE_FINAL && P.even_only) P.disp[(size_t)(y >> 1) * (P.W >> 1) + (x >> 1)] = d;
         else P.disp[p] = d;
     }
 }
@@ -209,8 +218,13 @@ template <int DPL, int MODE, int SAT, bool KEY16>
 __global__ void __launch_bounds__(128)
 k_path(const LineParams P) {
     constexpr int NR = DPL / 2;
-    constexpr int R = 4;   // input ring: steps whose loads are in flight
+    constexpr int K = Ring<DPL>::K, SBM = Ring<DPL>::SBM, NGB = Ring<DPL>::NGB;
+    constexpr int NPL = Planes<MODE>::N;
+    constexpr bool HAS_S = Slot<DPL, MODE>::HAS_S;
+    constexpr int SLOT = Slot<DPL, MODE>::BYTES;
     using In = StepIn<DPL, MODE>;
+    extern __shared__ __align__(16) uint8_t smem[];
+
     const int lane = threadIdx.x & 31;
     const int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int G = P.gpw, LPL = P.lpl;
@@ -220,7 +234,8 @@ k_path(const LineParams P) {
     if (G == 1) { g = 0; li = lane; gmask = kFull; }
     else { g = lane / LPL; li = lane - g * LPL; gmask = ((1u << LPL) - 1u) << (g * LPL); }
     const int line = warp * G + g;
-    const bool active = li < P.nl && line < P.nlines;
+    const bool has_d = li < P.nl;
+    const bool active = has_d && line < P.nlines;
     const int d0 = li * DPL;
     const bool lead = li == 0;
     const uint32_t m_lo = li == 0 ? 0x00003FFFu : 0u;           // d = -1 does not exist
@@ -244,31 +259,114 @@ k_path(const LineParams P) {
     const int step = dy * P.W + dx;
     int p = y * P.W + x;
 
-    In ring[R];
-    if (active) {
+    // ---- this lane's share of every chunk's copies ----
+    // Byte streams (C and the planes share offsets): 16-byte granule u = lane + 32*j
+    // of a chunk covers ring bytes [16u, 16u+16) = step u*16/SBM, lanes' bytes r = u*16 % SBM,
+    // which belong to group r/D at byte r%D of its D-byte run.
+    uint8_t *ring = smem + (threadIdx.x >> 5) * (NCH * SLOT);
+    const uint32_t ring_s = (uint32_t)__cvta_generic_to_shared(ring);
+    const int gD = G * P.D;
+    const long long adv = (long long)K * step * P.D;   // element advance per chunk (bytes of C)
+    long long goff[NGB];
+    int glim[NGB];
 #pragma unroll
-        for (int j = 0; j < R; j++)
-            if (j < len) fetch<DPL, MODE>(P, p + j * step, d0, ring[j]);
+    for (int j = 0; j < NGB; j++) {
+        const int b = (lane + 32 * j) * 16, k = b / SBM, r = b % SBM;
+        const int gg = min(r / P.D, 31), o = r - gg * P.D;
+        const int pg = __shfl_sync(kFull, p, (gg * LPL) & 31);
+        const int lg = __shfl_sync(kFull, len, (gg * LPL) & 31);
+        goff[j] = ((long long)pg + (long long)k * step) * P.D + o;
+        glim[j] = r < gD ? lg - k : 0;
+    }
+    long long soff[HAS_S ? 2 * NGB : 1];
+    int slim[HAS_S ? 2 * NGB : 1];
+    if (HAS_S) {
+#pragma unroll
+        for (int j = 0; j < 2 * NGB; j++) {
+            const int b = (lane + 32 * j) * 16, k = b / (2 * SBM), r = b % (2 * SBM);
+            const int gg = min(r / (2 * P.D), 31), o = r - gg * 2 * P.D;
+            const int pg = __shfl_sync(kFull, p, (gg * LPL) & 31);
+            const int lg = __shfl_sync(kFull, len, (gg * LPL) & 31);
+            soff[j] = ((long long)pg + (long long)k * step) * 2 * P.D + o;
+            slim[j] = r < 2 * gD ? lg - k : 0;
+        }
+    }
+    const uint8_t *pl[NPL > 0 ? NPL : 1];
+    if (NPL > 0) pl[0] = P.sc;
+    if (NPL == 3) { pl[1] = P.sc2; pl[2] = P.sc3; }
+
+    // Enqueues chunk c (steps c*K .. c*K+K-1) into ring slot c % NCH.
+    auto issue = [&](int c) {
+        const uint32_t dst = ring_s + (uint32_t)((c % NCH) * SLOT);
+        const int i0 = c * K;
+#pragma unroll
+        for (int j = 0; j < NGB; j++) {
+            if (i0 < glim[j]) {
+                const uint32_t db = dst + (uint32_t)((lane + 32 * j) * 16);
+                cp_async16(db, P.C + goff[j]);
+#pragma unroll
+                for (int q = 0; q < NPL; q++) cp_async16(db + (uint32_t)((1 + q) * K * SBM), pl[q] + goff[j]);
+            }
+            goff[j] += adv;
+        }
+        if (HAS_S) {
+#pragma unroll
+            for (int j = 0; j < 2 * NGB; j++) {
+                if (i0 < slim[j])
+                    cp_async16(dst + (uint32_t)((1 + NPL) * K * SBM + (lane + 32 * j) * 16),
+                               (const uint8_t *)P.S + soff[j]);
+                soff[j] += 2 * adv;
+            }
+        }
+        cp_async_commit();
+    };
+
+    const int nchunks = (maxlen + K - 1) / K;
+#pragma unroll
+    for (int c = 0; c < NCH - 1; c++) issue(c);
+
+    // this lane's output for the current pixel: sc bytes (SCRATCH) or S words (STORE, ACCUM)
+    uint8_t *out = nullptr;
+    long long out_step = 0;
+    if (MODE == MODE_SCRATCH) { out = P.sc + (long long)p * P.D + d0; out_step = (long long)step * P.D; }
+    if (MODE == MODE_STORE || MODE == MODE_ACCUM) {
+        out = (uint8_t *)(P.S + (long long)p * P.D + d0); out_step = (long long)step * P.D * 2;
     }
 
-    // first pixel of the line: L = C
-    uint32_t L[NR], c[NR];
+    // Lanes past the last disparity (D/DPL lanes short of a whole warp) read
+    // ring bytes that no copy writes: fill them with cost 255 once. Every real
+    // L is at most 254 (plain: 62 + P2) or saturated to 255 (multi-scale), and
+    // a pad lane's L is at least its cost, so a pad lane never lowers a minimum;
+    // its neighbours mask it out as d = D.
+    if (!has_d) {
 #pragma unroll
-    for (int j = 0; j < NR; j++) c[j] = kPadPk;
-    if (active) unpack_cost<DPL, MODE>(ring[0], c);
-    uint32_t t = c[0];
+        for (int sl = 0; sl < NCH; sl++)
 #pragma unroll
-    for (int j = 0; j < NR; j++) { L[j] = c[j]; t = vmin2(t, c[j]); }
-    uint32_t mn = __reduce_min_sync(gmask, fold2(t));   // packed (mn | mn << 16)
-    emit<DPL, MODE, KEY16>(P, p, x, y, d0, lead, gmask, active, L, ring[0]);
-    if (active && R < len) fetch<DPL, MODE>(P, p + R * step, d0, ring[0]);
+            for (int k = 0; k < K; k++)
+#pragma unroll
+                for (int b = 0; b < DPL; b++) ring[sl * SLOT + k * SBM + lane * DPL + b] = 0xFF;
+    }
+    __syncwarp();
 
-    // One recurrence step on pixel i, whose inputs are in `slot`; the slot is
-    // refilled with pixel i+R's inputs once this step is done with it.
-    auto body = [&](In &slot, int i) {
+    // lanes of lines that end before the warp's last step (diagonals)
+    const int minlen = (int)__reduce_min_sync(kFull, active ? (uint32_t)len : 0x7FFFFFFFu);
+
+    uint32_t L[NR];
+    uint32_t mn = 0;   // L_prev = 0, min_prev = 0: the first step yields L = C
+#pragma unroll
+    for (int j = 0; j < NR; j++) L[j] = has_d ? 0u : kPadPk;
+    x -= dx; y -= dy; p -= step;
+    if (MODE != MODE_FINAL && MODE != MODE_FINAL3) out -= out_step;
+
+    // One recurrence step on the next pixel of the line; FULL: every line of
+    // the warp has this pixel (no per-step length test).
+    auto step_once = [&](const In &s, int i, auto full_t) {
+        constexpr bool FULL = decltype(full_t)::value;
         x += dx; y += dy; p += step;
-        const bool live = active && i < len;
-        if (live) unpack_cost<DPL, MODE>(slot, c);
+        if (MODE != MODE_FINAL && MODE != MODE_FINAL3) out += out_step;
+        const bool live = FULL ? active : i < len;
+        uint32_t c[NR];
+        unpack_cost<DPL, MODE>(s, c);
         const uint32_t up = __shfl_up_sync(kFull, L[NR - 1], 1);
         const uint32_t dn = __shfl_down_sync(kFull, L[0], 1);
         const uint32_t lo0 = __byte_perm(up, L[NR - 1], 0x5432) | m_lo;   // (prev lane's last d, own d0+NR-1)
@@ -290,56 +388,107 @@ k_path(const LineParams P) {
             tm = vmin2(tm, v);
         }
         mn = __reduce_min_sync(gmask, fold2(tm));
-        emit<DPL, MODE, KEY16>(P, p, x, y, d0, lead, gmask, live, L, slot);
-        if (active && i + R < len) fetch<DPL, MODE>(P, p + R * step, d0, slot);
+        emit<DPL, MODE, KEY16>(P, out, p, x, y, d0, lead, gmask, live, L, s);
     };
 
-    // pixel i's inputs live in ring[i % R]
-    int i = 1;
-    for (; i + R - 1 < maxlen; i += R) {
-        body(ring[1], i);
-        body(ring[2], i + 1);
-        body(ring[3], i + 2);
-        body(ring[0], i + 3);
+    for (int ch = 0; ch < nchunks; ch++) {
+        cp_async_wait<NCH - 2>();   // chunk ch has landed (this lane's copies)
+        __syncwarp();               // ... and every lane's; slot ch-1 is free
+        issue(ch + NCH - 1);
+        const uint8_t *chunk = ring + (ch % NCH) * SLOT;
+        In s[K];                    // the chunk's inputs, read before its steps run
+#pragma unroll
+        for (int k = 0; k < K; k++) ring_read<DPL, MODE>(chunk, lane, k, s[k]);
+        if ((ch + 1) * K <= minlen) {
+#pragma unroll
+            for (int k = 0; k < K; k++) step_once(s[k], ch * K + k, std::true_type{});
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) step_once(s[k], ch * K + k, std::false_type{});
+        }
     }
-    if (i < maxlen) body(ring[1], i);
-    if (i + 1 < maxlen) body(ring[2], i + 1);
-    if (i + 2 < maxlen) body(ring[3], i + 2);
+    cp_async_wait<0>();   // no copy outlives the kernel
 }
 
 // ---------------------------------------------------------------------------
+template <int DPL, int MODE, int SAT, bool KEY16>
+static cudaError_t prep_one() {
+    return cudaFuncSetAttribute(k_path<DPL, MODE, SAT, KEY16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                4 * NCH * Slot<DPL, MODE>::BYTES);
+}
+
+template <int DPL, int SAT, bool KEY16>
+static cudaError_t prep_dpl() {
+    cudaError_t e;
+    if ((e = prep_one<DPL, MODE_SCRATCH, SAT, false>()) != cudaSuccess) return e;
+    if ((e = prep_one<DPL, MODE_STORE, SAT, false>()) != cudaSuccess) return e;
+    if ((e = prep_one<DPL, MODE_ACCUM, SAT, false>()) != cudaSuccess) return e;
+    if ((e = prep_one<DPL, MODE_FINAL, SAT, false>()) != cudaSuccess) return e;
+    return prep_one<DPL, MODE_FINAL3, SAT, KEY16>();
+}
+
+cudaError_t prepare_path_kernels() {
+    cudaError_t e;
+    if ((e = prep_dpl<2, 0, false>()) != cudaSuccess) return e;
+    if ((e = prep_dpl<2, 0, true>()) != cudaSuccess) return e;
+    if ((e = prep_dpl<4, 0, false>()) != cudaSuccess) return e;
+    if ((e = prep_dpl<4, 0, true>()) != cudaSuccess) return e;
+    if ((e = prep_dpl<8, 0, false>()) != cudaSuccess) return e;
+    if ((e = prep_dpl<2, 1, false>()) != cudaSuccess) return e;
+    if ((e = prep_dpl<4, 1, false>()) != cudaSuccess) return e;
+    return prep_dpl<8, 1, false>();
+}
+
 template <int DPL, int SAT, bool KEY16>
 static cudaError_t launch_path_mode(const LineParams &p, int mode, dim3 g, dim3 b, cudaStream_t s) {
+    const int w = (int)(b.x / 32);
     switch (mode) {
-    case MODE_SCRATCH: k_path<DPL, MODE_SCRATCH, SAT, false><<<g, b, 0, s>>>(p); break;
-    case MODE_STORE:   k_path<DPL, MODE_STORE, SAT, false><<<g, b, 0, s>>>(p); break;
-    case MODE_ACCUM:   k_path<DPL, MODE_ACCUM, SAT, false><<<g, b, 0, s>>>(p); break;
-    case MODE_FINAL:   k_path<DPL, MODE_FINAL, SAT, false><<<g, b, 0, s>>>(p); break;
-    case MODE_FINAL3:  k_path<DPL, MODE_FINAL3, SAT, KEY16><<<g, b, 0, s>>>(p); break;
+    case MODE_SCRATCH:
+        k_path<DPL, MODE_SCRATCH, SAT, false><<<g, b, w * NCH * Slot<DPL, MODE_SCRATCH>::BYTES, s>>>(p); break;
+    case MODE_STORE:
+        k_path<DPL, MODE_STORE, SAT, false><<<g, b, w * NCH * Slot<DPL, MODE_STORE>::BYTES, s>>>(p); break;
+    case MODE_ACCUM:
+        k_path<DPL, MODE_ACCUM, SAT, false><<<g, b, w * NCH * Slot<DPL, MODE_ACCUM>::BYTES, s>>>(p); break;
+    case MODE_FINAL:
+        k_path<DPL, MODE_FINAL, SAT, false><<<g, b, w * NCH * Slot<DPL, MODE_FINAL>::BYTES, s>>>(p); break;
+    case MODE_FINAL3:
+        k_path<DPL, MODE_FINAL3, SAT, KEY16><<<g, b, w * NCH * Slot<DPL, MODE_FINAL3>::BYTES, s>>>(p); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
+int path_dpl(int D, int want) {
+    if (D < 16 || D > 256 || D % 16) return 0;
+    const int lo = D <= 64 ? 2 : (D <= 128 ? 4 : 8);   // at most 32 lanes per line
+    if (want != 0 && want != 2 && want != 4 && want != 8) return 0;
+    return want < lo ? lo : want;
+}
+
 cudaError_t launch_line(const LineParams &p0, int mode, int saturate, int warps_per_block, cudaStream_t s) {
     LineParams p = p0;
     if (warps_per_block < 1 || warps_per_block > 4 || p.nlines < 1 || !p.C) return cudaErrorInvalidValue;
-    const int dpl = dpl_for(p.D);
-    if (!dpl) return cudaErrorInvalidValue;
+    const int dpl = path_dpl(p.D, p.dpl);
+    if (!dpl || p.D % dpl) return cudaErrorInvalidValue;
     p.nl = p.D / dpl;                      // lanes per line that hold disparities
     p.lpl = p.nl;
     p.gpw = (32 % p.lpl == 0) ? 32 / p.lpl : 1;
     const int lines_per_block = warps_per_block * p.gpw;
     const dim3 b(32 * warps_per_block), g((p.nlines + lines_per_block - 1) / lines_per_block);
-    const bool key16 = p.key16 != 0 && dpl == 2;
+    const bool key16 = p.key16 != 0 && p.D <= 64;
     if (saturate) {
-        if (dpl == 2) return launch_path_mode<2, 1, false>(p, mode, g, b, s);
-        return cudaErrorInvalidValue;
+        switch (dpl) {
+        case 2: return launch_path_mode<2, 1, false>(p, mode, g, b, s);
+        case 4: return launch_path_mode<4, 1, false>(p, mode, g, b, s);
+        case 8: return launch_path_mode<8, 1, false>(p, mode, g, b, s);
+        default: return cudaErrorInvalidValue;
+        }
     }
     switch (dpl) {
     case 2: return key16 ? launch_path_mode<2, 0, true>(p, mode, g, b, s)
                          : launch_path_mode<2, 0, false>(p, mode, g, b, s);
-    case 4: return launch_path_mode<4, 0, false>(p, mode, g, b, s);
+    case 4: return key16 ? launch_path_mode<4, 0, true>(p, mode, g, b, s)
+                         : launch_path_mode<4, 0, false>(p, mode, g, b, s);
     case 8: return launch_path_mode<8, 0, false>(p, mode, g, b, s);
     default: return cudaErrorInvalidValue;
     }

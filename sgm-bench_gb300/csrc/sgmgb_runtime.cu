@@ -103,6 +103,8 @@ static int ms_p1(int dx, int dy) { return dy == 0 ? 40 : (dx == 0 ? 20 : 10); }
 
 static cudaError_t run_paths(const LineParams &base, int paths, int sat, bool ms, int wpb,
                              cudaStream_t st) {
+    // passes run in order on one stream: each pair's first pass parks L in sc,
+    // its second adds it into S (the pair schedule of the 8-path sum)
     const PassSpec *ps = paths == 8 ? kPasses8 : kPasses4;
     for (int i = 0; i < paths; i++) {
         LineParams p = base;
@@ -116,9 +118,10 @@ static cudaError_t run_paths(const LineParams &base, int paths, int sat, bool ms
 }
 
 cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8_t *d_right,
-                          uint8_t *d_disp, cudaStream_t st, int wpb, cudaEvent_t ev_census,
-                          cudaEvent_t ev_end) {
+                          uint8_t *d_disp, cudaStream_t st, const PathShape &shape,
+                          cudaEvent_t ev_census, cudaEvent_t ev_end) {
     const sgmgb_frame_desc &fd = s.fd;
+    const int wpb = shape.wpb;
     cudaError_t e;
     if (fd.variant == SGMGB_PLAIN) {
         if ((e = launch_census2(d_left, d_right, s.cl, s.cr, fd.W, fd.H, st)) != cudaSuccess) return e;
@@ -127,7 +130,7 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
         LineParams p{};
         p.C = s.C; p.sc = s.sc; p.S = s.S; p.disp = d_disp;
-        p.W = fd.W; p.H = fd.H; p.D = fd.D; p.nl = fd.D / dpl_for(fd.D);
+        p.W = fd.W; p.H = fd.H; p.D = fd.D; p.dpl = shape.dpl;
         p.p2 = 192; p.even_only = 0; p.p1 = 20;
         p.key16 = (fd.paths == 4 && fd.D <= 64) ? 1 : 0;
         if (fd.paths == 8) {
@@ -173,12 +176,12 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
         LineParams p1{};
         p1.C = s.C1; p1.sc = s.sc; p1.S = s.S; p1.disp = s.disp1;
-        p1.W = hw; p1.H = hh; p1.D = 64; p1.nl = 32; p1.p2 = 200; p1.even_only = 0;
+        p1.W = hw; p1.H = hh; p1.D = 64; p1.dpl = shape.dpl; p1.p2 = 200; p1.even_only = 0;
         if ((e = run_paths(p1, 8, 1, true, wpb, st)) != cudaSuccess) return e;
         // stage 2: full scale, cost averaged with the half-scale cost (:183-199)
         LineParams p2{};
         p2.C = s.C; p2.sc = s.sc; p2.S = s.S; p2.disp = d_disp;
-        p2.W = W; p2.H = H; p2.D = 64; p2.nl = 32; p2.p2 = 200; p2.even_only = 1;
+        p2.W = W; p2.H = H; p2.D = 64; p2.dpl = shape.dpl; p2.p2 = 200; p2.even_only = 1;
         if ((e = run_paths(p2, 8, 1, true, wpb, st)) != cudaSuccess) return e;
     }
     if (ev_end && (e = cudaEventRecord(ev_end, st)) != cudaSuccess) return e;
@@ -257,12 +260,27 @@ int sgmgb_create(int device, sgmgb_ctx **out) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
+    if (e == cudaSuccess) e = prepare_path_kernels();
     if (e != cudaSuccess) {
         cudaGetLastError();
         sgmgb_destroy(ctx);
         return SGMGB_ERR_CUDA;
     }
     *out = ctx;
+    return SGMGB_OK;
+}
+
+int sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane) {
+    if (!ctx) return SGMGB_ERR_ARG;
+    if (warps_per_block < 1 || warps_per_block > 4)
+        return set_err(ctx, SGMGB_ERR_ARG, "warps_per_block must be 1..4");
+    if (disp_per_lane != 0 && disp_per_lane != 2 && disp_per_lane != 4 && disp_per_lane != 8)
+        return set_err(ctx, SGMGB_ERR_ARG, "disp_per_lane must be 0, 2, 4 or 8");
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    ctx->shape.wpb = warps_per_block;
+    ctx->shape.dpl = disp_per_lane;
     return SGMGB_OK;
 }
 
@@ -322,7 +340,7 @@ int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right, u
     const auto tB = clk::now();
     e = cudaEventRecord(ctx->ev[0], ctx->stream);
     if (e == cudaSuccess)
-        e = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, 4, ctx->ev[1], ctx->ev[2]);
+        e = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, ctx->shape, ctx->ev[1], ctx->ev[2]);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "frame pipeline");
     const auto tC = clk::now();
@@ -360,7 +378,7 @@ static cudaError_t capture_frame_graph(sgmgb_ctx *ctx, const uint8_t *l, const u
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    cudaError_t ee = enqueue_frame(*ctx->slot, l, r, d, ctx->stream, ctx->warps_per_block, nullptr, nullptr);
+    cudaError_t ee = enqueue_frame(*ctx->slot, l, r, d, ctx->stream, ctx->shape, nullptr, nullptr);
     e = cudaStreamEndCapture(ctx->stream, &g);
     if (ee != cudaSuccess) { if (g) cudaGraphDestroy(g); return ee; }
     if (e != cudaSuccess) return e;

@@ -25,7 +25,8 @@ OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_NODEV, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE 
 # every symbol include/sgmgb.h declares
 EXPORTS = [
     "sgmgb_abi_version", "sgmgb_strerror", "sgmgb_last_error", "sgmgb_check_desc", "sgmgb_out_size",
-    "sgmgb_workspace_bytes", "sgmgb_create", "sgmgb_destroy", "sgmgb_plan", "sgmgb_run_frame",
+    "sgmgb_workspace_bytes", "sgmgb_create", "sgmgb_destroy", "sgmgb_plan", "sgmgb_set_path_shape",
+    "sgmgb_run_frame",
     "sgmgb_run_frame_async", "sgmgb_sync", "sgmgb_census_async", "sgmgb_batch_create", "sgmgb_batch_run",
     "sgmgb_batch_tile_shape", "sgmgb_batch_destroy", "sgmgb_tune_lookup", "sgmgb_tune_record",
     "sgmgb_server_create", "sgmgb_server_add_camera", "sgmgb_server_submit", "sgmgb_server_poll",
@@ -80,6 +81,7 @@ def _load():
         "sgmgb_create": (i, [i, ctypes.POINTER(vp)]),
         "sgmgb_destroy": (None, [vp]),
         "sgmgb_plan": (i, [vp, fdp]),
+        "sgmgb_set_path_shape": (i, [vp, i, i]),
         "sgmgb_run_frame": (i, [vp, u8p, u8p, u8p, ctypes.POINTER(StageTimes)]),
         "sgmgb_run_frame_async": (i, [vp, u8p, u8p, u8p, vp]),
         "sgmgb_sync": (i, [vp, vp]),
@@ -208,6 +210,11 @@ class Engine:
     def plan(self, W, H, D=64, paths=4, variant=PLAIN):
         self.fd = desc(W, H, D, paths, variant)
         self._check(lib.sgmgb_plan(self.h, ctypes.byref(self.fd)))
+        return self
+
+    def set_path_shape(self, warps_per_block=4, disp_per_lane=0):
+        """Path-kernel shape (speed only; results are identical)."""
+        self._check(lib.sgmgb_set_path_shape(self.h, warps_per_block, disp_per_lane))
         return self
 
     def run_frame(self, left, right, times=False):

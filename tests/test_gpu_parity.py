@@ -106,6 +106,30 @@ def test_multiscale_synthetic(engine):
     assert np.array_equal(got, oracle.multiscale(left, right))
 
 
+# ---- path-kernel shapes: only speed may depend on them ----
+@pytest.mark.parametrize("wpb,dpl", [(1, 2), (2, 4), (3, 8), (4, 4), (4, 8)])
+def test_path_shapes(engine, wpb, dpl):
+    cases = [((97, 45), 64, 4, sgmgb.PLAIN), ((130, 66), 64, 8, sgmgb.PLAIN), ((61, 40), 16, 4, sgmgb.PLAIN),
+             ((300, 70), 48, 8, sgmgb.PLAIN), ((200, 33), 128, 4, sgmgb.PLAIN), ((130, 66), 64, 8, sgmgb.MULTISCALE)]
+    try:
+        engine.set_path_shape(wpb, dpl)
+        for (W, H), D, paths, variant in cases:
+            left, right, _ = sgmgb.synth_pair(W, H, D, seed=W + D)
+            engine.plan(W, H, D, paths, variant)
+            got = engine.run_frame(left, right)
+            want = oracle.multiscale(left, right) if variant else oracle.plain(left, right, D, paths)
+            assert np.array_equal(got, want), ("%dx%d D=%d paths=%d v=%d" % (W, H, D, paths, variant)
+                                               + _first_diff(got, want))
+    finally:
+        engine.set_path_shape(4, 0)
+
+
+def test_rejects_bad_path_shape(engine):
+    for wpb, dpl in ((0, 2), (5, 2), (4, 3), (4, 16), (4, -1)):
+        with pytest.raises(sgmgb.SgmError):
+            engine.set_path_shape(wpb, dpl)
+
+
 def test_rejects_bad_descriptions(engine):
     for args in ((0, 10, 64, 4, 0), (10, 10, 65, 4, 0), (10, 10, 272, 4, 0), (10, 10, 64, 6, 0),
                  (11, 10, 64, 8, 1), (10, 10, 128, 8, 1), (10, 10, 64, 4, 1)):
