@@ -109,19 +109,45 @@ int sgmgb_census_async(sgmgb_ctx *ctx, const uint8_t *d_img, uint64_t *d_out, in
                        void *stream);
 
 /* ---- batch: many frames of mixed sizes in one persistent launch ---- */
+/* A batch runs n plain-variant frames of any sizes, disparity ranges and path
+ * counts in ONE persistent kernel launch: its blocks take work items (census
+ * row bands, cost row bands, groups of lines of one direction) from a device
+ * queue in phase order and wait, with a bounded spin, on per-frame phase
+ * counters. The launch and its counter resets are captured in a CUDA graph on
+ * the first run and replayed afterwards. Outputs are bit-identical to
+ * sgmgb_run_frame on each frame. */
 typedef struct sgmgb_batch sgmgb_batch;
-/* Plans n frames: workspace per frame, the per-frame tile queue, the tile
- * shape (autotuned per frame shape and cached), and a CUDA graph of the
- * whole batch. */
+/* Plans n frames: one workspace arena, the work-item queue and its phase
+ * counters. tune_cache (may be NULL) is an autotuner cache file (see below):
+ * each frame takes the path-kernel shape recorded for its description, and the
+ * launch the warps per block recorded for the largest frame; otherwise 4 warps
+ * and the smallest valid disparities per lane. */
 int  sgmgb_batch_create(sgmgb_ctx *ctx, const sgmgb_frame_desc *frames, int n,
-                        sgmgb_batch **out);
-/* Runs the planned batch on device buffers (arrays of n pointers, host
- * arrays of device pointers). Enqueued on `stream`; returns without waiting. */
+                        const char *tune_cache, sgmgb_batch **out);
+/* Runs the planned batch on device buffers (host arrays of n device pointers:
+ * left/right W*H bytes, disp W*H bytes), enqueued on `stream` (NULL = the
+ * context's stream); returns without waiting. */
 int  sgmgb_batch_run(sgmgb_batch *b, const uint8_t *const *d_left,
                      const uint8_t *const *d_right, uint8_t *const *d_disp, void *stream);
-/* Path-kernel shape chosen for frame i: warps per block and disparities per lane. */
+/* Waits for the last run: SGMGB_OK, or SGMGB_ERR_TIMEOUT when a work item's
+ * wait for its inputs ran past the wait limit (the run was abandoned and the
+ * outputs are undefined; the context stays usable). */
+int  sgmgb_batch_wait(sgmgb_batch *b);
+/* Times candidate shapes (warps per block 2 and 4; disparities per lane the
+ * smallest valid and twice that) on these buffers, keeps the fastest, and,
+ * when tune_cache is not NULL, records it for every frame description. */
+int  sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left,
+                          const uint8_t *const *d_right, uint8_t *const *d_disp,
+                          const char *tune_cache);
+/* Path-kernel shape used for frame i: warps per block and disparities per lane. */
 int  sgmgb_batch_tile_shape(const sgmgb_batch *b, int i, int *warps_per_block,
                             int *disp_per_lane);
+/* Failure injection for tests (host side; nothing faults on the device):
+ * wait_limit_ms bounds every device-side wait (default 2000); stall_frame >= 0
+ * raises that frame's census completion target by one, so the frame's cost
+ * items wait until the limit and the next run reports SGMGB_ERR_TIMEOUT.
+ * stall_frame = -1 clears it. */
+int  sgmgb_batch_set_fault(sgmgb_batch *b, int wait_limit_ms, int stall_frame);
 void sgmgb_batch_destroy(sgmgb_batch *b);
 
 /* ---- autotuner cache (host-only; no GPU needed) ---- */

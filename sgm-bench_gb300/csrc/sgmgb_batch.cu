@@ -1,8 +1,617 @@
-// sgmgb_batch.cu -- placeholder until the persistent batch launch lands.
+// sgmgb_batch.cu -- many frames of mixed sizes in one persistent launch.
+//
+// Work decomposition (plain variant, common/sgm_ref.c semantics per frame):
+//   phase 0  census   one item per band of BAND rows (both images)
+//   phase 1  cost     one item per band: C[p][d] from the band's census rows
+//   4 paths: phase 2  R->L, B->T, L->R into three u8 planes (all three passes)
+//            phase 3  T->B adds the planes to its L and takes the argmin
+//   8 paths: phase 2+k  pass k of the pair schedule (sc / S), k = 0..7
+// An item of phase k of frame f starts when every item of phase k-1 of f has
+// finished. Items are queued phase-major over all frames, so while one frame
+// waits at a phase boundary the others keep the SMs busy; every item's
+// dependencies sit earlier in the queue, so a block never waits on an item
+// that no running block holds.
+//
+// Cross-block data (census, cost, planes, sums) is read through L2 only
+// (cp.async.cg, ld.global.cg): a block never reads such data through its L1.
 #include "sgmgb_internal.h"
-extern "C" {
-int sgmgb_batch_create(sgmgb_ctx *, const sgmgb_frame_desc *, int, sgmgb_batch **out) { if (out) *out = nullptr; return SGMGB_ERR_STATE; }
-int sgmgb_batch_run(sgmgb_batch *, const uint8_t *const *, const uint8_t *const *, uint8_t *const *, void *) { return SGMGB_ERR_STATE; }
-int sgmgb_batch_tile_shape(const sgmgb_batch *, int, int *, int *) { return SGMGB_ERR_STATE; }
-void sgmgb_batch_destroy(sgmgb_batch *) {}
+#include "sgmgb_path.cuh"
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+namespace sgmgb {
+
+namespace {
+
+constexpr int BAND = 4;          // rows per census / cost item
+constexpr int TX = 64;           // columns per census / cost tile
+constexpr int MAXPH = 10;        // phases per frame (8 paths: census, cost, 8 passes)
+
+enum ItemKind : int { IT_CENSUS = 0, IT_COST = 1, IT_PATH = 2 };
+
+struct BFrame {                  // per frame; the user pointers are refreshed per run
+    const uint8_t *left, *right;
+    uint8_t *disp;
+    uint64_t *cl, *cr;
+    uint8_t *C;
+    int W, H, D;
+};
+
+struct BPass {                   // one direction of one frame
+    LineParams P;                // C, planes, S, W, H, D, nl/lpl/gpw, dx, dy, p1, p2, nlines, key16
+    int frame;
+    int mode;
+    int dpl;
+};
+
+struct BItem {
+    int kind;
+    int frame;
+    int phase;                   // this item's phase
+    int arg;                     // band (census, cost) or pass index (path)
+    int sub;                     // path: first warp of the item
+};
+
+struct BCtl {                    // device control block, reset before every run
+    unsigned next;               // queue head
+    unsigned abort;              // set on a wait timeout: every block stops taking items
+    int err_item;                // item whose wait ran out (-1: none)
+    unsigned pad;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
 }
+
+// Thread 0 only: waits until *cnt >= need, the run is aborted, or the limit
+// passes (then records the item and aborts the run). Returns false if the
+// item must not run.
+__device__ bool wait_count(const unsigned *cnt, unsigned need, BCtl *ctl, int item,
+                           long long limit_cycles) {
+    if (ld_acquire(cnt) >= need) return true;
+    const long long t0 = clock64();
+    for (unsigned it = 0;; it++) {
+        if (ld_acquire(&ctl->abort)) return false;
+        if (ld_acquire(cnt) >= need) return true;
+        if (clock64() - t0 > limit_cycles || it > (1u << 26)) {
+            atomicCAS(&ctl->err_item, -1, item);
+            atomicExch(&ctl->abort, 1u);
+            return false;
+        }
+        __nanosleep(it < 64 ? 64 : 512);
+    }
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Census 9x7 of rows [y0, y0+BAND) of both images (common/sgm_ref.c:23-41),
+// staged through shared memory one TX-column tile at a time.
+__device__ void item_census(const BFrame &F, int band, uint8_t *sm) {
+    const int W = F.W, H = F.H, y0 = band * BAND, nt = blockDim.x;
+    constexpr int TW = TX + 8, TH = BAND + 6;
+    for (int img = 0; img < 2; img++) {
+        const uint8_t *im = img ? F.right : F.left;
+        uint64_t *out = img ? F.cr : F.cl;
+        for (int x0 = 0; x0 < W; x0 += TX) {
+            for (int i = threadIdx.x; i < TW * TH; i += nt) {
+                const int ty = i / TW, tx = i - ty * TW;
+                sm[i] = __ldg(im + (size_t)clampi(y0 + ty - 3, 0, H - 1) * W + clampi(x0 + tx - 4, 0, W - 1));
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < TX * BAND; i += nt) {
+                const int ty = i / TX, tx = i - ty * TX, x = x0 + tx, y = y0 + ty;
+                if (x < W && y < H) {
+                    const uint8_t *c = sm + (ty + 3) * TW + (tx + 4);
+                    const uint32_t cv = *c;
+                    uint64_t bits = 0;
+                    int n = 0;
+#pragma unroll
+                    for (int dy = -3; dy <= 3; dy++)
+#pragma unroll
+                        for (int dx = -4; dx <= 4; dx++) {
+                            if (dx == 0 && dy == 0) continue;
+                            bits |= (uint64_t)(c[dy * TW + dx] < cv) << n;
+                            n++;
+                        }
+                    out[(size_t)y * W + x] = bits;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Cost C[(y*W + x)*D + d] = popcount(cl[x] ^ cr[x-d]), 62 where x - d < 0
+// (common/sgm_ref.c:44-56), for rows [y0, y0+BAND). Per TX-column tile the
+// left descriptors and the right ones from D-1 columns before the tile are
+// staged in shared memory; each thread makes 8 disparities of one pixel.
+__device__ void item_cost(const BFrame &F, int band, uint8_t *smb) {
+    const int W = F.W, H = F.H, D = F.D, y0 = band * BAND, nt = blockDim.x;
+    uint64_t *sl = (uint64_t *)smb;         // TX left descriptors
+    uint64_t *sr = sl + TX;                 // D-1+TX right descriptors, sr[j] = cr[x0 - (D-1) + j]
+    const int tpp = D >> 3;                 // threads per pixel
+    for (int y = y0; y < min(y0 + BAND, H); y++) {
+        const uint64_t *cl = F.cl + (size_t)y * W, *cr = F.cr + (size_t)y * W;
+        for (int x0 = 0; x0 < W; x0 += TX) {
+            for (int i = threadIdx.x; i < TX + D - 1 + TX; i += nt) {
+                if (i < TX) {
+                    sl[i] = x0 + i < W ? __ldcg(cl + x0 + i) : 0;
+                } else {
+                    const int j = i - TX, x = x0 - (D - 1) + j;
+                    sr[j] = (x >= 0 && x < W) ? __ldcg(cr + x) : 0;
+                }
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < TX * tpp; t += nt) {
+                const int px = t / tpp, d0 = (t - px * tpp) * 8, x = x0 + px;
+                if (x < W) {
+                    const uint64_t a = sl[px];
+                    uint32_t v[8];
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        const int d = d0 + k;
+                        v[k] = x - d >= 0 ? (uint32_t)__popcll(a ^ sr[px + (D - 1) - d]) : (uint32_t)kInvalidPlain;
+                    }
+                    const uint32_t lo = v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24);
+                    const uint32_t hi = v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24);
+                    *(uint2 *)(F.C + ((size_t)y * W + x) * D + d0) = make_uint2(lo, hi);
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// One warp's share of a path item: lines of warp `warp` of pass `bp`.
+__device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int warp, uint8_t *ring) {
+    LineParams P = bp.P;
+    P.disp = disp;
+    const bool key16 = P.key16 && P.D <= 64;
+    switch (bp.dpl * 8 + bp.mode) {
+    case 2 * 8 + MODE_SCRATCH: path_warp<2, MODE_SCRATCH, 0, false>(P, warp, ring); break;
+    case 2 * 8 + MODE_STORE:   path_warp<2, MODE_STORE, 0, false>(P, warp, ring); break;
+    case 2 * 8 + MODE_ACCUM:   path_warp<2, MODE_ACCUM, 0, false>(P, warp, ring); break;
+    case 2 * 8 + MODE_FINAL:   path_warp<2, MODE_FINAL, 0, false>(P, warp, ring); break;
+    case 2 * 8 + MODE_FINAL3:
+        if (key16) path_warp<2, MODE_FINAL3, 0, true>(P, warp, ring);
+        else path_warp<2, MODE_FINAL3, 0, false>(P, warp, ring);
+        break;
+    case 4 * 8 + MODE_SCRATCH: path_warp<4, MODE_SCRATCH, 0, false>(P, warp, ring); break;
+    case 4 * 8 + MODE_STORE:   path_warp<4, MODE_STORE, 0, false>(P, warp, ring); break;
+    case 4 * 8 + MODE_ACCUM:   path_warp<4, MODE_ACCUM, 0, false>(P, warp, ring); break;
+    case 4 * 8 + MODE_FINAL:   path_warp<4, MODE_FINAL, 0, false>(P, warp, ring); break;
+    case 4 * 8 + MODE_FINAL3:
+        if (key16) path_warp<4, MODE_FINAL3, 0, true>(P, warp, ring);
+        else path_warp<4, MODE_FINAL3, 0, false>(P, warp, ring);
+        break;
+    case 8 * 8 + MODE_SCRATCH: path_warp<8, MODE_SCRATCH, 0, false>(P, warp, ring); break;
+    case 8 * 8 + MODE_STORE:   path_warp<8, MODE_STORE, 0, false>(P, warp, ring); break;
+    case 8 * 8 + MODE_ACCUM:   path_warp<8, MODE_ACCUM, 0, false>(P, warp, ring); break;
+    case 8 * 8 + MODE_FINAL:   path_warp<8, MODE_FINAL, 0, false>(P, warp, ring); break;
+    case 8 * 8 + MODE_FINAL3:  path_warp<8, MODE_FINAL3, 0, false>(P, warp, ring); break;
+    default: break;
+    }
+}
+
+// The persistent batch kernel: every block loops taking the next queued item
+// until the queue is empty or the run is aborted. `ring_bytes`: one warp's
+// path ring; the census and cost items use the start of the block's memory.
+__global__ void __launch_bounds__(256)
+k_batch(const BItem *__restrict__ items, int n_items, const BFrame *__restrict__ frames,
+        const BPass *__restrict__ passes, unsigned *done, const unsigned *__restrict__ need,
+        BCtl *ctl, int ring_bytes, long long limit_cycles) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ int s_item;
+    const int wib = threadIdx.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int it = ld_acquire(&ctl->abort) ? n_items : (int)atomicAdd(&ctl->next, 1u);
+            if (it < n_items) {
+                const BItem I = items[it];
+                if (I.phase > 0) {
+                    const int c = I.frame * MAXPH + I.phase - 1;
+                    if (!wait_count(&done[c], need[c], ctl, it, limit_cycles)) it = n_items;
+                }
+            }
+            s_item = it;
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n_items) break;
+        const BItem I = items[it];
+        switch (I.kind) {
+        case IT_CENSUS: item_census(frames[I.frame], I.arg, smem); break;
+        case IT_COST:   item_cost(frames[I.frame], I.arg, smem); break;
+        default:        item_path(passes[I.arg], frames[I.frame].disp, I.sub + wib, smem + wib * ring_bytes); break;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(&done[I.frame * MAXPH + I.phase], 1u);
+        }
+    }
+}
+
+template <int DPL, int MODE> constexpr int ring_of() { return Slot<DPL, MODE>::RING; }
+
+// Largest per-warp ring a pass of this shape needs.
+int ring_bytes_for(int dpl, int mode) {
+    switch (dpl * 8 + mode) {
+    case 2 * 8 + MODE_SCRATCH: return ring_of<2, MODE_SCRATCH>();
+    case 2 * 8 + MODE_STORE:   return ring_of<2, MODE_STORE>();
+    case 2 * 8 + MODE_ACCUM:   return ring_of<2, MODE_ACCUM>();
+    case 2 * 8 + MODE_FINAL:   return ring_of<2, MODE_FINAL>();
+    case 2 * 8 + MODE_FINAL3:  return ring_of<2, MODE_FINAL3>();
+    case 4 * 8 + MODE_SCRATCH: return ring_of<4, MODE_SCRATCH>();
+    case 4 * 8 + MODE_STORE:   return ring_of<4, MODE_STORE>();
+    case 4 * 8 + MODE_ACCUM:   return ring_of<4, MODE_ACCUM>();
+    case 4 * 8 + MODE_FINAL:   return ring_of<4, MODE_FINAL>();
+    case 4 * 8 + MODE_FINAL3:  return ring_of<4, MODE_FINAL3>();
+    case 8 * 8 + MODE_SCRATCH: return ring_of<8, MODE_SCRATCH>();
+    case 8 * 8 + MODE_STORE:   return ring_of<8, MODE_STORE>();
+    case 8 * 8 + MODE_ACCUM:   return ring_of<8, MODE_ACCUM>();
+    case 8 * 8 + MODE_FINAL:   return ring_of<8, MODE_FINAL>();
+    case 8 * 8 + MODE_FINAL3:  return ring_of<8, MODE_FINAL3>();
+    default: return 0;
+    }
+}
+
+}  // namespace
+}  // namespace sgmgb
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+using namespace sgmgb;
+
+struct sgmgb_batch {
+    sgmgb_ctx *ctx = nullptr;
+    int n = 0;
+    std::vector<sgmgb_frame_desc> fds;
+    std::vector<int> dpl;                 // per frame (resolved, >= smallest valid)
+    int wpb = 4;
+    // device memory
+    void *arena = nullptr;                // all frames' workspaces
+    size_t arena_bytes = 0;
+    std::vector<FrameSlot> slots;         // carved pointers (host copy)
+    void *tables = nullptr;               // frames | passes | items | done | need | ctl
+    BFrame *d_frames = nullptr;
+    BPass *d_passes = nullptr;
+    BItem *d_items = nullptr;
+    unsigned *d_done = nullptr, *d_need = nullptr;
+    BCtl *d_ctl = nullptr;
+    int n_items = 0, n_passes = 0;
+    int ring_bytes = 0;
+    size_t smem_bytes = 0;
+    int grid = 0;
+    std::vector<unsigned> need;
+    // pinned host staging
+    BFrame *h_frames = nullptr;           // pointer table copied in by every run
+    BCtl *h_ctl = nullptr;                // [0]: reset image, [1]: read back after the run
+    // graph of [table copy, counter reset, kernel, control read-back]
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t done_ev = nullptr;
+    bool ran = false;
+    int wait_limit_ms = 2000;
+    int stall_frame = -1;
+};
+
+namespace {
+
+int berr(sgmgb_batch *b, int code, const std::string &msg) { return set_err(b ? b->ctx : nullptr, code, msg); }
+
+void free_tables(sgmgb_batch *b) {
+    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    if (b->tables) { cudaFree(b->tables); b->tables = nullptr; }
+}
+
+// Builds passes, items and completion targets for the current shapes and
+// uploads them; drops the graph.
+int build_plan(sgmgb_batch *b) {
+    cudaSetDevice(b->ctx->device);
+    if (b->ran) cudaEventSynchronize(b->done_ev);
+    free_tables(b);
+    std::vector<BPass> passes;
+    std::vector<std::vector<BItem>> by_phase(MAXPH);
+    b->need.assign((size_t)b->n * MAXPH, 0u);
+    int ring = 0;
+    for (int f = 0; f < b->n; f++) {
+        const sgmgb_frame_desc &fd = b->fds[f];
+        const FrameSlot &s = b->slots[f];
+        const int nb = (fd.H + BAND - 1) / BAND;
+        for (int k = 0; k < nb; k++) {
+            by_phase[0].push_back({IT_CENSUS, f, 0, k, 0});
+            by_phase[1].push_back({IT_COST, f, 1, k, 0});
+        }
+        b->need[(size_t)f * MAXPH + 0] = nb;
+        b->need[(size_t)f * MAXPH + 1] = nb;
+        LineParams base{};
+        base.C = s.C; base.sc = s.sc; base.S = s.S; base.disp = nullptr;
+        base.W = fd.W; base.H = fd.H; base.D = fd.D; base.p1 = 20; base.p2 = 192;
+        base.key16 = (fd.paths == 4 && fd.D <= 64) ? 1 : 0;
+        const int dpl = b->dpl[f];
+        base.dpl = dpl;
+        base.nl = fd.D / dpl; base.lpl = base.nl; base.gpw = (32 % base.lpl == 0) ? 32 / base.lpl : 1;
+        struct Spec { int dx, dy, mode, phase; uint8_t *sc; const uint8_t *sc2, *sc3; };
+        std::vector<Spec> specs;
+        if (fd.paths == 4) {
+            const size_t plane = (size_t)fd.W * fd.H * fd.D;
+            uint8_t *pl[3] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane};
+            specs.push_back({-1, 0, MODE_SCRATCH, 2, pl[0], nullptr, nullptr});
+            specs.push_back({0, -1, MODE_SCRATCH, 2, pl[1], nullptr, nullptr});
+            specs.push_back({1, 0, MODE_SCRATCH, 2, pl[2], nullptr, nullptr});
+            specs.push_back({0, 1, MODE_FINAL3, 3, pl[0], pl[1], pl[2]});
+        } else {
+            static const int sched[8][3] = {{-1, 0, MODE_SCRATCH}, {1, 0, MODE_STORE}, {0, -1, MODE_SCRATCH},
+                                            {0, 1, MODE_ACCUM}, {-1, -1, MODE_SCRATCH}, {1, 1, MODE_ACCUM},
+                                            {1, -1, MODE_SCRATCH}, {-1, 1, MODE_FINAL}};
+            for (int k = 0; k < 8; k++) specs.push_back({sched[k][0], sched[k][1], sched[k][2], 2 + k, s.sc, nullptr, nullptr});
+        }
+        for (const Spec &sp : specs) {
+            BPass bp{};
+            bp.P = base;
+            bp.P.dx = sp.dx; bp.P.dy = sp.dy;
+            bp.P.sc = sp.sc; bp.P.sc2 = sp.sc2; bp.P.sc3 = sp.sc3;
+            bp.P.nlines = lines_for(fd.W, fd.H, sp.dx, sp.dy);
+            bp.frame = f; bp.mode = sp.mode; bp.dpl = dpl;
+            const int pi = (int)passes.size();
+            passes.push_back(bp);
+            ring = std::max(ring, ring_bytes_for(dpl, sp.mode));
+            const int warps = (bp.P.nlines + bp.P.gpw - 1) / bp.P.gpw;
+            const int nit = (warps + b->wpb - 1) / b->wpb;
+            for (int j = 0; j < nit; j++) by_phase[sp.phase].push_back({IT_PATH, f, sp.phase, pi, j * b->wpb});
+            b->need[(size_t)f * MAXPH + sp.phase] += nit;
+        }
+    }
+    if (b->stall_frame >= 0 && b->stall_frame < b->n) b->need[(size_t)b->stall_frame * MAXPH + 0] += 1;
+    std::vector<BItem> items;
+    for (auto &v : by_phase) items.insert(items.end(), v.begin(), v.end());
+    b->n_items = (int)items.size();
+    b->n_passes = (int)passes.size();
+    b->ring_bytes = ring;
+    // census tile (72 x 10 bytes) and cost tile (2*TX + D - 1 descriptors) fit in any ring
+    size_t smem = (size_t)ring * b->wpb;
+    smem = std::max(smem, (size_t)(2 * TX + 256) * 8);
+    b->smem_bytes = smem;
+    // one device allocation for all tables
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t o_fr = 0, o_pa = o_fr + al(sizeof(BFrame) * b->n), o_it = o_pa + al(sizeof(BPass) * passes.size());
+    const size_t o_dn = o_it + al(sizeof(BItem) * items.size()), o_nd = o_dn + al(sizeof(unsigned) * b->need.size());
+    const size_t o_ct = o_nd + al(sizeof(unsigned) * b->need.size()), total = o_ct + al(sizeof(BCtl));
+    cudaError_t e = cudaMalloc(&b->tables, total);
+    if (e != cudaSuccess) { cudaGetLastError(); b->tables = nullptr; return berr(b, SGMGB_ERR_NOMEM, "batch tables"); }
+    uint8_t *t = (uint8_t *)b->tables;
+    b->d_frames = (BFrame *)(t + o_fr); b->d_passes = (BPass *)(t + o_pa); b->d_items = (BItem *)(t + o_it);
+    b->d_done = (unsigned *)(t + o_dn); b->d_need = (unsigned *)(t + o_nd); b->d_ctl = (BCtl *)(t + o_ct);
+    e = cudaMemcpy(b->d_passes, passes.data(), sizeof(BPass) * passes.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_items, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_need, b->need.data(), sizeof(unsigned) * b->need.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 32 * b->wpb, smem);
+    if (e != cudaSuccess) { cudaGetLastError(); return berr(b, SGMGB_ERR_CUDA, std::string("batch plan: ") + cudaGetErrorString(e)); }
+    if (per_sm < 1) return berr(b, SGMGB_ERR_ARG, "batch shape does not fit on an SM");
+    b->grid = per_sm * b->ctx->sm_count;
+    return SGMGB_OK;
+}
+
+// Fills the pinned pointer table for these buffers.
+void fill_frames(sgmgb_batch *b, const uint8_t *const *l, const uint8_t *const *r, uint8_t *const *d) {
+    for (int f = 0; f < b->n; f++) {
+        const FrameSlot &s = b->slots[f];
+        BFrame &F = b->h_frames[f];
+        F.left = l[f]; F.right = r[f]; F.disp = d[f];
+        F.cl = s.cl; F.cr = s.cr; F.C = s.C;
+        F.W = b->fds[f].W; F.H = b->fds[f].H; F.D = b->fds[f].D;
+    }
+}
+
+int capture_graph(sgmgb_batch *b) {
+    cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { cudaGetLastError(); return berr(b, SGMGB_ERR_CUDA, "batch capture"); }
+    int clock_khz = 0;
+    cudaDeviceGetAttribute(&clock_khz, cudaDevAttrClockRate, b->ctx->device);
+    if (clock_khz <= 0) clock_khz = 2000000;
+    const long long limit = (long long)b->wait_limit_ms * clock_khz;
+    cudaMemcpyAsync(b->d_frames, b->h_frames, sizeof(BFrame) * b->n, cudaMemcpyHostToDevice, b->cap);
+    cudaMemsetAsync(b->d_done, 0, sizeof(unsigned) * b->need.size(), b->cap);
+    cudaMemcpyAsync(b->d_ctl, &b->h_ctl[0], sizeof(BCtl), cudaMemcpyHostToDevice, b->cap);
+    k_batch<<<b->grid, 32 * b->wpb, b->smem_bytes, b->cap>>>(b->d_items, b->n_items, b->d_frames, b->d_passes,
+                                                             b->d_done, b->d_need, b->d_ctl, b->ring_bytes, limit);
+    cudaMemcpyAsync(&b->h_ctl[1], b->d_ctl, sizeof(BCtl), cudaMemcpyDeviceToHost, b->cap);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->cap, &g);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) { cudaGetLastError(); b->graph = nullptr; return berr(b, SGMGB_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e)); }
+    return SGMGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sgmgb_batch_create(sgmgb_ctx *ctx, const sgmgb_frame_desc *frames, int n, const char *tune_cache,
+                       sgmgb_batch **out) {
+    if (!ctx || !frames || n < 1 || !out) return SGMGB_ERR_ARG;
+    *out = nullptr;
+    for (int f = 0; f < n; f++) {
+        if (sgmgb_check_desc(&frames[f]) != SGMGB_OK)
+            return set_err(ctx, SGMGB_ERR_ARG, "batch frame " + std::to_string(f) + ": invalid description");
+        if (frames[f].variant != SGMGB_PLAIN)
+            return set_err(ctx, SGMGB_ERR_ARG, "batch frame " + std::to_string(f) + ": batches run the plain variant");
+    }
+    sgmgb_batch *b = new (std::nothrow) sgmgb_batch();
+    if (!b) return SGMGB_ERR_NOMEM;
+    b->ctx = ctx;
+    b->n = n;
+    b->fds.assign(frames, frames + n);
+    b->dpl.resize(n);
+    size_t biggest = 0;
+    for (int f = 0; f < n; f++) {
+        const sgmgb_frame_desc &fd = frames[f];
+        int w = 0, d = 0;
+        const bool hit = tune_cache && sgmgb_tune_lookup(tune_cache, &fd, &w, &d) == SGMGB_OK;
+        b->dpl[f] = path_dpl(fd.D, hit ? d : 0);
+        const size_t sz = (size_t)fd.W * fd.H * fd.D;
+        if (hit && sz > biggest) { biggest = sz; b->wpb = w; }
+    }
+    cudaSetDevice(ctx->device);
+    b->slots.resize(n);
+    std::vector<size_t> off(n);
+    size_t total = 0;
+    for (int f = 0; f < n; f++) { off[f] = total; total += (slot_layout(b->fds[f], nullptr) + 255) & ~(size_t)255; }
+    cudaError_t e = cudaMalloc(&b->arena, total);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b->arena = nullptr;
+        sgmgb_batch_destroy(b);
+        return set_err(ctx, SGMGB_ERR_NOMEM, "batch workspace of " + std::to_string(total) + " bytes");
+    }
+    b->arena_bytes = total;
+    for (int f = 0; f < n; f++) {
+        b->slots[f].fd = b->fds[f];
+        b->slots[f].base = (uint8_t *)b->arena + off[f];
+        slot_layout(b->fds[f], &b->slots[f]);
+    }
+    e = cudaHostAlloc((void **)&b->h_frames, sizeof(BFrame) * n, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&b->h_ctl, sizeof(BCtl) * 2, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        sgmgb_batch_destroy(b);
+        return set_err(ctx, SGMGB_ERR_CUDA, std::string("batch setup: ") + cudaGetErrorString(e));
+    }
+    memset(b->h_frames, 0, sizeof(BFrame) * n);
+    b->h_ctl[0] = BCtl{0u, 0u, -1, 0u};
+    b->h_ctl[1] = BCtl{0u, 0u, -1, 0u};
+    const int rc = build_plan(b);
+    if (rc) { sgmgb_batch_destroy(b); return rc; }
+    *out = b;
+    return SGMGB_OK;
+}
+
+int sgmgb_batch_run(sgmgb_batch *b, const uint8_t *const *d_left, const uint8_t *const *d_right,
+                    uint8_t *const *d_disp, void *stream) {
+    if (!b || !d_left || !d_right || !d_disp) return SGMGB_ERR_ARG;
+    for (int f = 0; f < b->n; f++)
+        if (!d_left[f] || !d_right[f] || !d_disp[f]) return berr(b, SGMGB_ERR_ARG, "batch frame " + std::to_string(f) + ": null buffer");
+    cudaSetDevice(b->ctx->device);
+    if (b->ran) cudaEventSynchronize(b->done_ev);   // the pinned table is read by the previous run
+    fill_frames(b, d_left, d_right, d_disp);
+    if (!b->graph) {
+        const int rc = capture_graph(b);
+        if (rc) return rc;
+    }
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->ctx->stream;
+    cudaError_t e = cudaGraphLaunch(b->graph, st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->done_ev, st);
+    if (e != cudaSuccess) { cudaGetLastError(); return berr(b, SGMGB_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e)); }
+    b->ran = true;
+    return SGMGB_OK;
+}
+
+int sgmgb_batch_wait(sgmgb_batch *b) {
+    if (!b) return SGMGB_ERR_ARG;
+    if (!b->ran) return SGMGB_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaError_t e = cudaEventSynchronize(b->done_ev);
+    if (e != cudaSuccess) { cudaGetLastError(); return berr(b, SGMGB_ERR_CUDA, std::string("batch run: ") + cudaGetErrorString(e)); }
+    if (b->h_ctl[1].err_item != -1)
+        return berr(b, SGMGB_ERR_TIMEOUT, "batch item " + std::to_string(b->h_ctl[1].err_item) + " waited past " +
+                                              std::to_string(b->wait_limit_ms) + " ms for its inputs; run abandoned");
+    return SGMGB_OK;
+}
+
+int sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left, const uint8_t *const *d_right,
+                         uint8_t *const *d_disp, const char *tune_cache) {
+    if (!b) return SGMGB_ERR_ARG;
+    cudaSetDevice(b->ctx->device);
+    const int saved_wpb = b->wpb;
+    const std::vector<int> saved_dpl = b->dpl;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess) {
+        cudaGetLastError();
+        if (t0) cudaEventDestroy(t0);
+        return berr(b, SGMGB_ERR_CUDA, "autotune events");
+    }
+    float best = -1.f;
+    int best_w = saved_wpb, best_m = 1, rc = SGMGB_OK;
+    for (int w : {2, 4}) {
+        for (int m : {1, 2}) {
+            b->wpb = w;
+            for (int f = 0; f < b->n; f++) b->dpl[f] = path_dpl(b->fds[f].D, std::min(8, path_dpl(b->fds[f].D, 0) * m));
+            if ((rc = build_plan(b))) goto done;
+            if ((rc = sgmgb_batch_run(b, d_left, d_right, d_disp, nullptr)) || (rc = sgmgb_batch_wait(b))) goto done;
+            float ms = 1e30f;
+            for (int rep = 0; rep < 3; rep++) {
+                cudaEventRecord(t0, b->ctx->stream);
+                if ((rc = sgmgb_batch_run(b, d_left, d_right, d_disp, nullptr))) goto done;
+                cudaEventRecord(t1, b->ctx->stream);
+                if ((rc = sgmgb_batch_wait(b))) goto done;
+                float t = 0.f;
+                cudaEventElapsedTime(&t, t0, t1);
+                ms = std::min(ms, t);
+            }
+            if (best < 0.f || ms < best) { best = ms; best_w = w; best_m = m; }
+        }
+    }
+done:
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (rc) {
+        b->wpb = saved_wpb;
+        b->dpl = saved_dpl;
+        build_plan(b);
+        return rc;
+    }
+    b->wpb = best_w;
+    for (int f = 0; f < b->n; f++) b->dpl[f] = path_dpl(b->fds[f].D, std::min(8, path_dpl(b->fds[f].D, 0) * best_m));
+    if ((rc = build_plan(b))) return rc;
+    if (tune_cache) {
+        for (int f = 0; f < b->n; f++) {
+            bool seen = false;
+            for (int g = 0; g < f && !seen; g++) seen = !memcmp(&b->fds[g], &b->fds[f], sizeof(sgmgb_frame_desc));
+            if (!seen && sgmgb_tune_record(tune_cache, &b->fds[f], b->wpb, b->dpl[f], 1000.0 * best) != SGMGB_OK)
+                return berr(b, SGMGB_ERR_STATE, std::string("cannot append to tune cache ") + tune_cache);
+        }
+    }
+    return SGMGB_OK;
+}
+
+int sgmgb_batch_tile_shape(const sgmgb_batch *b, int i, int *warps_per_block, int *disp_per_lane) {
+    if (!b || i < 0 || i >= b->n) return SGMGB_ERR_ARG;
+    if (warps_per_block) *warps_per_block = b->wpb;
+    if (disp_per_lane) *disp_per_lane = b->dpl[i];
+    return SGMGB_OK;
+}
+
+int sgmgb_batch_set_fault(sgmgb_batch *b, int wait_limit_ms, int stall_frame) {
+    if (!b || wait_limit_ms < 1 || wait_limit_ms > 600000 || stall_frame < -1 || stall_frame >= b->n)
+        return SGMGB_ERR_ARG;
+    b->wait_limit_ms = wait_limit_ms;
+    b->stall_frame = stall_frame;
+    return build_plan(b);
+}
+
+void sgmgb_batch_destroy(sgmgb_batch *b) {
+    if (!b) return;
+    if (b->ctx) cudaSetDevice(b->ctx->device);
+    if (b->ran && b->done_ev) cudaEventSynchronize(b->done_ev);
+    free_tables(b);
+    if (b->arena) cudaFree(b->arena);
+    if (b->h_frames) cudaFreeHost(b->h_frames);
+    if (b->h_ctl) cudaFreeHost(b->h_ctl);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    if (b->done_ev) cudaEventDestroy(b->done_ev);
+    delete b;
+}
+
+}  // extern "C"

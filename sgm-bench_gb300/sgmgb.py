@@ -28,7 +28,8 @@ EXPORTS = [
     "sgmgb_workspace_bytes", "sgmgb_create", "sgmgb_destroy", "sgmgb_plan", "sgmgb_set_path_shape",
     "sgmgb_run_frame",
     "sgmgb_run_frame_async", "sgmgb_sync", "sgmgb_census_async", "sgmgb_batch_create", "sgmgb_batch_run",
-    "sgmgb_batch_tile_shape", "sgmgb_batch_destroy", "sgmgb_tune_lookup", "sgmgb_tune_record",
+    "sgmgb_batch_wait", "sgmgb_batch_autotune", "sgmgb_batch_tile_shape", "sgmgb_batch_set_fault",
+    "sgmgb_batch_destroy", "sgmgb_tune_lookup", "sgmgb_tune_record",
     "sgmgb_server_create", "sgmgb_server_add_camera", "sgmgb_server_submit", "sgmgb_server_poll",
     "sgmgb_server_wait", "sgmgb_server_stats_get", "sgmgb_server_destroy", "sgmgb_synth_pair",
 ]
@@ -86,9 +87,13 @@ def _load():
         "sgmgb_run_frame_async": (i, [vp, u8p, u8p, u8p, vp]),
         "sgmgb_sync": (i, [vp, vp]),
         "sgmgb_census_async": (i, [vp, u8p, vp, i, i, vp]),
-        "sgmgb_batch_create": (i, [vp, fdp, i, ctypes.POINTER(vp)]),
+        "sgmgb_batch_create": (i, [vp, fdp, i, ctypes.c_char_p, ctypes.POINTER(vp)]),
         "sgmgb_batch_run": (i, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), vp]),
+        "sgmgb_batch_wait": (i, [vp]),
+        "sgmgb_batch_autotune": (i, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                     ctypes.c_char_p]),
         "sgmgb_batch_tile_shape": (i, [vp, i, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "sgmgb_batch_set_fault": (i, [vp, i, i]),
         "sgmgb_batch_destroy": (None, [vp]),
         "sgmgb_tune_lookup": (i, [ctypes.c_char_p, fdp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "sgmgb_tune_record": (i, [ctypes.c_char_p, fdp, i, i, ctypes.c_double]),
@@ -126,6 +131,10 @@ def _ptr(x):
     if hasattr(x, "data_ptr"):
         return x.data_ptr()
     raise TypeError("cannot take the address of %r" % type(x))
+
+
+def _cstr(s):
+    return None if s is None else os.fsencode(s)
 
 
 def _stream(s):
@@ -244,26 +253,42 @@ class Engine:
 
 
 class Batch:
-    """Many frames of mixed shapes planned once and run as one persistent launch."""
+    """Many plain-variant frames of mixed shapes planned once and run as one
+    persistent launch (replayed as a CUDA graph)."""
 
-    def __init__(self, engine, descs):
+    def __init__(self, engine, descs, tune_cache=None):
         self.engine = engine
         self.n = len(descs)
+        self.descs = list(descs)
         arr = (FrameDesc * self.n)(*descs)
         h = ctypes.c_void_p()
-        engine._check(lib.sgmgb_batch_create(engine.h, arr, self.n, ctypes.byref(h)))
+        engine._check(lib.sgmgb_batch_create(engine.h, arr, self.n, _cstr(tune_cache), ctypes.byref(h)))
         self.h = h
 
-    def run(self, d_lefts, d_rights, d_disps, stream=None):
+    def _arrays(self, d_lefts, d_rights, d_disps):
         A = ctypes.c_void_p * self.n
-        rc = lib.sgmgb_batch_run(self.h, A(*[_ptr(x) for x in d_lefts]), A(*[_ptr(x) for x in d_rights]),
-                                 A(*[_ptr(x) for x in d_disps]), _stream(stream))
-        self.engine._check(rc)
+        return (A(*[_ptr(x) for x in d_lefts]), A(*[_ptr(x) for x in d_rights]), A(*[_ptr(x) for x in d_disps]))
+
+    def run(self, d_lefts, d_rights, d_disps, stream=None):
+        """Enqueues the batch on device buffers; returns without waiting."""
+        self.engine._check(lib.sgmgb_batch_run(self.h, *self._arrays(d_lefts, d_rights, d_disps), _stream(stream)))
+
+    def wait(self):
+        """Waits for the last run; raises SgmError(ERR_TIMEOUT) if it was abandoned."""
+        self.engine._check(lib.sgmgb_batch_wait(self.h))
+
+    def autotune(self, d_lefts, d_rights, d_disps, tune_cache=None):
+        self.engine._check(lib.sgmgb_batch_autotune(self.h, *self._arrays(d_lefts, d_rights, d_disps),
+                                                    _cstr(tune_cache)))
 
     def tile_shape(self, i):
-        w, l = ctypes.c_int(), ctypes.c_int()
-        self.engine._check(lib.sgmgb_batch_tile_shape(self.h, i, ctypes.byref(w), ctypes.byref(l)))
-        return w.value, l.value
+        """(warps per block, disparities per lane) used for frame i."""
+        w, d = ctypes.c_int(), ctypes.c_int()
+        self.engine._check(lib.sgmgb_batch_tile_shape(self.h, i, ctypes.byref(w), ctypes.byref(d)))
+        return w.value, d.value
+
+    def set_fault(self, wait_limit_ms=2000, stall_frame=-1):
+        self.engine._check(lib.sgmgb_batch_set_fault(self.h, wait_limit_ms, stall_frame))
 
     def close(self):
         if self.h:

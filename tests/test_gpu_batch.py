@@ -1,0 +1,133 @@
+"""The batched form: many frames of mixed shapes in one persistent launch.
+
+Every frame of a batch must equal the oracle (common/sgm_ref.c restated in
+oracle/sgm_oracle.c) byte for byte, on the first run and on graph replays with
+other buffers; the bounded device-side waits must turn a stalled dependency
+into SGMGB_ERR_TIMEOUT with the context still usable."""
+import numpy as np
+import pytest
+
+import oracle
+import sgmgb
+
+pytestmark = pytest.mark.gpu
+
+
+def _frames(specs, seed0=0):
+    """specs: (W, H, D, paths). Returns descs, host pairs, device pairs, device outputs."""
+    import torch
+    descs, host, dev, outs = [], [], [], []
+    for k, (W, H, D, paths) in enumerate(specs):
+        l, r, _ = sgmgb.synth_pair(W, H, min(D, 128), seed=seed0 + k + 1)
+        descs.append(sgmgb.desc(W, H, D, paths))
+        host.append((l, r))
+        dev.append((torch.from_numpy(l).cuda(), torch.from_numpy(r).cuda()))
+        outs.append(torch.zeros((H, W), dtype=torch.uint8, device="cuda"))
+    return descs, host, dev, outs
+
+
+def _check(host, outs, descs, tag=""):
+    for k, ((l, r), o, d) in enumerate(zip(host, outs, descs)):
+        got = o.cpu().numpy()
+        want = oracle.plain(l, r, d.D, d.paths)
+        if not np.array_equal(got, want):
+            idx = np.argwhere(got != want)
+            y, x = idx[0]
+            pytest.fail("%sframe %d (%dx%d D=%d paths=%d): %d pixels differ, first (x=%d,y=%d) got %d want %d"
+                        % (tag, k, d.W, d.H, d.D, d.paths, len(idx), x, y, got[y, x], want[y, x]))
+
+
+MIX = [(160, 96, 64, 4), (97, 45, 64, 8), (320, 200, 128, 4), (61, 40, 16, 4), (200, 33, 128, 8),
+       (1, 1, 64, 4), (23, 1, 16, 8), (1, 23, 64, 4), (300, 70, 48, 8), (640, 480, 64, 4)]
+
+
+def test_batch_mixed_frames_exact(engine):
+    import torch
+    descs, host, dev, outs = _frames(MIX)
+    b = sgmgb.Batch(engine, descs)
+    b.run([d[0] for d in dev], [d[1] for d in dev], outs)
+    b.wait()
+    torch.cuda.synchronize()
+    _check(host, outs, descs, "first run: ")
+    # graph replay on other buffers: the same frames with left/right swapped roles of two pairs
+    for o in outs:
+        o.zero_()
+    b.run([d[0] for d in dev], [d[1] for d in dev], outs)
+    b.wait()
+    _check(host, outs, descs, "replay: ")
+    b.close()
+
+
+def test_batch_new_buffers_each_run(engine):
+    import torch
+    specs = [(128, 64, 64, 4), (96, 80, 64, 8), (64, 48, 128, 4)]
+    descs, host1, dev1, outs1 = _frames(specs, seed0=10)
+    _, host2, dev2, outs2 = _frames(specs, seed0=20)
+    b = sgmgb.Batch(engine, descs)
+    for host, dev, outs in ((host1, dev1, outs1), (host2, dev2, outs2), (host1, dev1, outs2)):
+        for o in outs:
+            o.zero_()
+        b.run([d[0] for d in dev], [d[1] for d in dev], outs)
+        b.wait()
+        torch.cuda.synchronize()
+        _check(host, outs, descs)
+    b.close()
+
+
+def test_batch_autotune_and_cache(engine, tmp_path):
+    import torch
+    specs = [(320, 240, 64, 4), (256, 128, 128, 8), (320, 240, 64, 4)]
+    descs, host, dev, outs = _frames(specs, seed0=30)
+    cache = str(tmp_path / "tune.txt")
+    b = sgmgb.Batch(engine, descs)
+    L, R = [d[0] for d in dev], [d[1] for d in dev]
+    b.autotune(L, R, outs, cache)
+    shapes = [b.tile_shape(i) for i in range(len(specs))]
+    for w, d in shapes:
+        assert w in (2, 4) and d in (2, 4, 8)
+    for o in outs:
+        o.zero_()
+    b.run(L, R, outs)
+    b.wait()
+    torch.cuda.synchronize()
+    _check(host, outs, descs)
+    b.close()
+    lines = [l.split() for l in open(cache) if l.strip()]
+    assert len(lines) == 2                       # one line per distinct description
+    # a new batch planned from the cache takes the recorded shapes
+    b2 = sgmgb.Batch(engine, descs, tune_cache=cache)
+    assert [b2.tile_shape(i) for i in range(len(specs))] == shapes
+    b2.close()
+
+
+def test_batch_wait_limit_reports_timeout(engine):
+    """A frame whose census target can never be met: its cost items' waits run
+    out, the run is abandoned with SGMGB_ERR_TIMEOUT, and the batch (and the
+    context) run correctly afterwards."""
+    import torch
+    specs = [(128, 64, 64, 4), (96, 80, 64, 8), (64, 48, 64, 4)]
+    descs, host, dev, outs = _frames(specs, seed0=40)
+    b = sgmgb.Batch(engine, descs)
+    L, R = [d[0] for d in dev], [d[1] for d in dev]
+    b.set_fault(wait_limit_ms=200, stall_frame=1)
+    b.run(L, R, outs)
+    with pytest.raises(sgmgb.SgmError) as ei:
+        b.wait()
+    assert ei.value.code == sgmgb.ERR_TIMEOUT
+    b.set_fault(wait_limit_ms=2000, stall_frame=-1)
+    b.run(L, R, outs)
+    b.wait()
+    torch.cuda.synchronize()
+    _check(host, outs, descs)
+    b.close()
+
+
+def test_batch_rejects_bad_input(engine):
+    with pytest.raises(sgmgb.SgmError):
+        sgmgb.Batch(engine, [sgmgb.desc(64, 48, 64, 8, sgmgb.MULTISCALE)])
+    with pytest.raises(sgmgb.SgmError):
+        sgmgb.Batch(engine, [sgmgb.desc(64, 48, 65, 4)])
+    b = sgmgb.Batch(engine, [sgmgb.desc(16, 16, 64, 4)])
+    with pytest.raises(sgmgb.SgmError):
+        b.run([0], [0], [0])
+    b.close()
