@@ -302,6 +302,68 @@ class Batch:
             pass
 
 
+class Server:
+    """The served form: cameras with resident slots, frames admitted as they
+    arrive (HBM budget, in-flight limit), results collected by ticket."""
+
+    def __init__(self, engine, hbm_budget_bytes=40 << 30, max_inflight=8, streams=8):
+        self.engine = engine
+        cfg = ServerConfig(hbm_budget_bytes, max_inflight, streams)
+        h = ctypes.c_void_p()
+        engine._check(lib.sgmgb_server_create(engine.h, ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.cams = {}
+
+    def add_camera(self, cam_id, W, H, D=64, paths=4, variant=PLAIN):
+        fd = desc(W, H, D, paths, variant)
+        self.engine._check(lib.sgmgb_server_add_camera(self.h, cam_id, ctypes.byref(fd)))
+        self.cams[cam_id] = fd
+
+    def submit(self, cam_id, left, right):
+        left = np.ascontiguousarray(left, np.uint8)
+        right = np.ascontiguousarray(right, np.uint8)
+        t = ctypes.c_uint64()
+        self.engine._check(lib.sgmgb_server_submit(self.h, cam_id, left.ctypes.data, right.ctypes.data,
+                                                   ctypes.byref(t)))
+        return t.value, cam_id
+
+    def _out(self, cam_id):
+        fd = self.cams[cam_id]
+        ow, oh = out_size(fd.W, fd.H, fd.D, fd.paths, fd.variant)
+        return np.empty((oh, ow), np.uint8)
+
+    def poll(self, ticket):
+        """(True, disp, latency_ms) when done, else (False, None, None)."""
+        t, cam = ticket
+        out, lat = self._out(cam), ctypes.c_double()
+        rc = lib.sgmgb_server_poll(self.h, t, out.ctypes.data, ctypes.byref(lat))
+        if rc < 0:
+            self.engine._check(rc)
+        return (True, out, lat.value) if rc == 1 else (False, None, None)
+
+    def wait(self, ticket, timeout_ms=10000):
+        t, cam = ticket
+        out, lat = self._out(cam), ctypes.c_double()
+        self.engine._check(lib.sgmgb_server_wait(self.h, t, out.ctypes.data, ctypes.byref(lat), timeout_ms))
+        return out, lat.value
+
+    def stats(self):
+        st = ServerStats()
+        self.engine._check(lib.sgmgb_server_stats_get(self.h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def close(self):
+        if self.h:
+            lib.sgmgb_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Plugin:
     """A built sgm.h plugin library; calls its SGM_IMPL.run like the reference harness."""
 
