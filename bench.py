@@ -125,6 +125,21 @@ def dist_setup():
     return ws, rank, local
 
 
+def max_over_ranks(v, dist, device):
+    """The largest of each rank's v (the slowest rank's time); v itself on one process."""
+    if dist is None:
+        return float(v)
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ws, frames_per_rank, seconds):
+    """Whole-job MDE/s: every rank's frames over the slowest rank's time."""
+    return ws * frames_per_rank * W * H * D / seconds / 1e6
+
+
 def cpu_baseline_sample(seconds=12.0):
     """The oracle, one thread, on whole frames of the workload (at least one)."""
     import oracle
@@ -237,13 +252,9 @@ def run_gb300(args):
     barrier()
     tw1 = time.time()
     clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
     ms_per_step = ms / args.steps
-    value = ws * args.steps * W * H * D / (ms / 1e3) / 1e6
+    value = replica_value(ws, args.steps, ms / 1e3)
 
     # end to end through the host-buffer call: pinned inputs in, map out, every step
     hl = [torch.from_numpy(p[0]).pin_memory().numpy() for p in pairs]
@@ -259,12 +270,8 @@ def run_gb300(args):
         a = time.perf_counter()
         eng.run_frame(hl[i % R], hr[i % R])
         lat.append(time.perf_counter() - a)
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = ws * e2e_steps * W * H * D / e2e_s / 1e6
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    e2e_value = replica_value(ws, e2e_steps, e2e_s)
     _, st = eng.run_frame(hl[0], hr[0], times=True)
 
     if rank != 0:
