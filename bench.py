@@ -3,16 +3,23 @@
 4 paths, bit-exact), in MDE/s (W*H*D / second), with frames/s beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--no-batch] [--no-serve]
 
 One step is one frame through the engine. `value` is measured with the
 inputs already resident on the device (one CUDA-graph launch per frame,
-round-robin over 8 distinct synthetic pairs); `e2e` is the same metric
-through the host-buffer call (sgmgb_run_frame: pinned host inputs copied in,
-the disparity map copied back, every step). `roofline` relates the modelled
-minimal bytes of a frame (2*W*H*D + 3*W*H) to its device time and the
-measured HBM copy bandwidth. `cpu_baseline` is the CPU oracle on a bounded
-sample of the same workload, one thread. `--impl reference` times the CPU
-oracle (the reference's algorithm, restated in C) on all host threads.
+round-robin over 8 distinct synthetic pairs whose working set is far larger
+than L2); `e2e` is the same metric through the host-buffer call
+(sgmgb_run_frame: pinned host inputs copied in, the disparity map copied
+back, every step). `roofline` is the dominant kernel's: its algorithmic bytes
+per launch over its mean launch time (CUDA events, kernel alone), against the
+measured HBM copy bandwidth; `frame_roofline` relates the modelled minimal
+bytes of a frame (2*W*H*D + 3*W*H) to the pipelined frame time. `batched`
+runs the 96-pair mixed batch in one persistent launch against 96 sequential
+drop-in calls; `served` drives 8 virtual cameras with Poisson arrivals at
+2000 frames/s through the server and reports p50/p99 latency.
+`cpu_baseline` is the CPU oracle on a bounded sample of the same workload, one
+thread. `--impl reference` times the CPU oracle (the reference's algorithm,
+restated in C) on all host threads.
 
 Multi-GPU: frames are independent, so N GPUs run N replicas (one process per
 GPU under torchrun); `value` is the frames of all ranks over the slowest
@@ -49,13 +56,15 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per frame from the committed ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", "configA_frame_traffic.txt")
+def committed_traffic(kernel):
+    """DRAM bytes (read + write) of one launch of `kernel` at configuration A,
+    from the committed ncu summary (lines "traffic <kernel> <bytes>"), or None."""
+    path = os.path.join(ROOT, "profiles", "configA_kernel_traffic.txt")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_frame:"):
-                return int(line.split(":")[1].split()[0])
+            f = line.split()
+            if len(f) >= 3 and f[0] == "traffic" and f[1] == kernel:
+                return int(f[2])
     except Exception:
         pass
     return None
@@ -138,6 +147,123 @@ def max_over_ranks(v, dist, device):
 def replica_value(ws, frames_per_rank, seconds):
     """Whole-job MDE/s: every rank's frames over the slowest rank's time."""
     return ws * frames_per_rank * W * H * D / seconds / 1e6
+
+
+def batched_section(eng_cls, sgmgb, torch, np):
+    """The batched form on the 96-pair mix (24 each at 640x480, 1280x720,
+    1920x800, 1920x1080; D 64/128 alternating; every 4th pair 8-path) against
+    96 sequential plain drop-in calls (host buffers, one pre-planned context
+    per frame description, so no re-planning is timed)."""
+    sizes = [(640, 480), (1280, 720), (1920, 800), (1920, 1080)]
+    specs = [(W, H, 64 if k % 2 == 0 else 128, 8 if k % 4 == 3 else 4) for (W, H) in sizes for k in range(24)]
+    scenes = {}
+    for (W, H, Dk, P) in specs:
+        if (W, H, Dk) not in scenes:
+            scenes[(W, H, Dk)] = sgmgb.synth_pair(W, H, Dk, seed=W + Dk)[:2]
+    host = [scenes[(W, H, Dk)] for (W, H, Dk, P) in specs]
+    dl = [torch.from_numpy(l).cuda() for l, r in host]
+    dr = [torch.from_numpy(r).cuda() for l, r in host]
+    out = [torch.zeros((H, W), dtype=torch.uint8, device="cuda") for (W, H, Dk, P) in specs]
+    eng = eng_cls(0)
+    b = sgmgb.Batch(eng, [sgmgb.desc(*sp) for sp in specs])
+    b.autotune(dl, dr, out)
+    b.run(dl, dr, out)
+    b.wait()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record()
+    for _ in range(reps):
+        b.run(dl, dr, out)
+    e1.record()
+    b.wait()
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1) / reps
+    engs = {sp: eng_cls(0).plan(*sp) for sp in set(specs)}
+    ref = [engs[sp].run_frame(l, r) for sp, (l, r) in zip(specs, host)]        # warm-up and reference maps
+    t0 = time.perf_counter()
+    for sp, (l, r) in zip(specs, host):
+        engs[sp].run_frame(l, r)
+    seq_ms = (time.perf_counter() - t0) * 1e3
+    same = all(np.array_equal(o.cpu().numpy(), rf) for o, rf in zip(out, ref))
+    shapes = sorted(set(b.tile_shape(i) for i in range(len(specs))))
+    for e in engs.values():
+        e.close()
+    b.close()
+    eng.close()
+    mde = sum(W * H * Dk for (W, H, Dk, P) in specs)
+    return {"frames": len(specs), "ms_per_batch": batch_ms, "fps": 96e3 / batch_ms,
+            "mde_per_s": mde / (batch_ms / 1e3) / 1e6,
+            "sequential_dropin_ms": seq_ms, "sequential_dropin_fps": 96e3 / seq_ms,
+            "speedup_vs_sequential_dropin": seq_ms / batch_ms, "identical_to_dropin": bool(same),
+            "launches_per_batch": 1, "tile_shapes_warps_dpl": shapes,
+            "note": "one persistent launch per batch (CUDA graph); batch inputs resident on the device; "
+                    "drop-in calls copy host buffers in and out"}
+
+
+def served_section(eng_cls, sgmgb, np, rate=2000.0, secs=3.0):
+    """8 virtual cameras (sizes from 640x480 / 1280x720 / 1920x1080, D 64/128,
+    4-path), Poisson arrivals at `rate` frames/s in aggregate, 40 GB budget."""
+    import queue
+    rng = np.random.default_rng(0)
+    sizes = [(640, 480), (1280, 720), (1920, 1080)]
+    cams = {c: sizes[rng.integers(0, 3)] + (int(rng.choice([64, 128])), 4) for c in range(8)}
+    scenes, want = {}, {}
+    for c, (W, H, Dk, P) in cams.items():
+        scenes[c] = [sgmgb.synth_pair(W, H, Dk, seed=1000 + 10 * c + k)[:2] for k in range(2)]
+        e = eng_cls(0).plan(W, H, Dk, P)
+        want[c] = [e.run_frame(l, r) for l, r in scenes[c]]
+        e.close()
+    eng = eng_cls(0)
+    srv = sgmgb.Server(eng, hbm_budget_bytes=40 << 30, max_inflight=8)
+    for c, (W, H, Dk, P) in cams.items():
+        srv.add_camera(c, W, H, Dk, P)
+    q = queue.Queue()
+    refused = [0]
+
+    def producer():
+        t_next = time.perf_counter()
+        t_end = t_next + secs
+        i = 0
+        while True:
+            t_next += rng.exponential(1.0 / rate)
+            if t_next > t_end:
+                break
+            while time.perf_counter() < t_next:
+                pass
+            c = int(rng.integers(0, 8))
+            try:
+                q.put((srv.submit(c, *scenes[c][i % 2]), c, i % 2))
+            except sgmgb.SgmError:
+                refused[0] += 1
+            i += 1
+        q.put(None)
+
+    bad = [0]
+
+    def consumer():
+        while True:
+            it = q.get()
+            if it is None:
+                return
+            t, c, k = it
+            o, _ = srv.wait(t, 60000)
+            bad[0] += int(not np.array_equal(o, want[c][k]))
+
+    th = [threading.Thread(target=producer), threading.Thread(target=consumer)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    st = srv.stats()
+    srv.close()
+    eng.close()
+    return {"cameras": {str(c): "%dx%d D=%d" % v[:3] for c, v in cams.items()}, "offered_fps": rate,
+            "seconds": secs, "frames_done": st["frames_done"], "frames_refused": st["frames_refused"],
+            "fps": st["fps"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+            "resident_gb": st["resident_bytes"] / 1e9, "budget_gb": 40 * 2 ** 30 / 1e9,
+            "results_differing_from_alone": bad[0],
+            "latency": "submit (host copy into pinned memory) to result in pinned host memory"}
 
 
 def cpu_baseline_sample(seconds=12.0):
@@ -274,14 +400,19 @@ def run_gb300(args):
     e2e_value = replica_value(ws, e2e_steps, e2e_s)
     _, st = eng.run_frame(hl[0], hr[0], times=True)
 
+    # per-kernel device time, each kernel alone, CUDA events on the engine's stream
+    kstats = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
+
     if rank != 0:
         eng.close()
         if dist is not None:
             dist.destroy_process_group()
         return 0
     peak, peak_kind = peaks()
-    achieved = B_ALG / (ms_per_step / 1e3) / 1e9
-    traffic = committed_traffic()
+    top = max(kstats, key=lambda k: k[1])
+    achieved = top[2] / (top[1] / 1e3) / 1e9
+    traffic = committed_traffic(top[0])
+    frame_ms_alone = sum(k[1] for k in kstats)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -295,17 +426,28 @@ def run_gb300(args):
                 "fps": ws * e2e_steps / e2e_s, "p50_ms": statistics.median(lat) * 1e3,
                 "p99_ms": sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
                 "stage_ms": {k: round(v, 4) for k, v in st.items() if k.endswith("_ms")}},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "note": "one launch = one CUDA-graph launch of the frame pipeline (census + %d path "
-                             "passes); achieved = %d modelled bytes / device time; peak %s" % (
-                                 PATHS, B_ALG, peak_kind)},
+        "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": top[2],
+                     "launch_ms": top[1],
+                     "note": "dominant kernel of the frame (longest mean launch, timed alone with CUDA events); "
+                             "achieved = its algorithmic bytes per launch / that time; peak = %s HBM copy "
+                             "bandwidth; traffic = ncu dram bytes of one launch (profiles/)" % peak_kind},
+        "frame_roofline": {"modelled_bytes": B_ALG, "achieved": B_ALG / (ms_per_step / 1e3) / 1e9,
+                           "frac": B_ALG / (ms_per_step / 1e3) / 1e9 / peak, "unit": "GB/s",
+                           "note": "B_alg = 2*W*H*D + 3*W*H over the pipelined frame time (ms_per_step)"},
+        "kernels": [{"name": k[0], "ms": round(k[1], 5), "algorithmic_bytes": k[2],
+                     "gbs": round(k[2] / (k[1] / 1e3) / 1e9, 1)} for k in kstats],
+        "frame_ms_kernels_alone": frame_ms_alone,
         "cpu_baseline": cpu_baseline_sample(args.cpu_seconds),
         "clocks": clocks.summary(tw0, tw1),
         "gpu_launches": args.steps * KERNELS_PER_FRAME,
     }
-    print(json.dumps(line))
     eng.close()
+    if not args.no_batch:
+        line["batched"] = batched_section(sgmgb.Engine, sgmgb, torch, np)
+    if not args.no_serve:
+        line["served"] = served_section(sgmgb.Engine, sgmgb, np)
+    print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
     return 0
@@ -320,6 +462,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--warps-per-block", type=int, default=4, help="path-kernel shape (speed only)")
     ap.add_argument("--disp-per-lane", type=int, default=0, help="path-kernel shape: 0, 2, 4 or 8")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-form section")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-form section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

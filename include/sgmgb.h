@@ -103,6 +103,19 @@ int sgmgb_run_frame_async(sgmgb_ctx *ctx, const uint8_t *d_left, const uint8_t *
 /* Waits for everything the context enqueued on `stream` (NULL = own stream). */
 int sgmgb_sync(sgmgb_ctx *ctx, void *stream);
 
+/* ---- measurement (no reference symbol) ---- */
+typedef struct {
+    char   name[24];   /* "census", "cost", "path_rl", "path_tb_final", ... */
+    double ms;         /* mean device time of one launch (CUDA events) */
+    double bytes;      /* algorithmic bytes of one launch: inputs read once, outputs written once */
+} sgmgb_kernel_stat;
+/* Runs `reps` frames of the planned description on device buffers with every
+ * kernel alone on the context's stream (no concurrent passes) and CUDA events
+ * around each launch; fills up to max_out per-kernel means in launch order and
+ * sets *n_out. Synchronous. */
+int sgmgb_profile_frame(sgmgb_ctx *ctx, const uint8_t *d_left, const uint8_t *d_right, uint8_t *d_disp,
+                        int reps, sgmgb_kernel_stat *out, int max_out, int *n_out);
+
 /* ---- component entry points (parity tests, tools) ---- */
 /* 9x7 census of one W x H image on the device; out is W*H uint64. */
 int sgmgb_census_async(sgmgb_ctx *ctx, const uint8_t *d_img, uint64_t *d_out, int W, int H,

@@ -64,12 +64,23 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s /* may be null: size
 int  slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err);
 void slot_free(FrameSlot *s);
 
+// Per-kernel timing of one enqueued frame: ev[0] before the first launch,
+// ev[i+1] after launch i (timing-enabled events, created by the caller).
+struct KernelProbe {
+    static constexpr int kMax = 24;
+    int n = 0;
+    cudaEvent_t ev[kMax + 1] = {};
+    const char *name[kMax] = {};
+    double bytes[kMax] = {};
+};
+
 // Enqueues the whole frame pipeline for `s` reading d_left/d_right and
 // writing d_disp on `st`. Events ev_census / ev_end (optional) are recorded
-// after the cost volume and at the end.
+// after the cost volume and at the end. With a probe, every kernel runs on
+// `st` one after another and the probe's events bracket each launch.
 cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8_t *d_right,
                           uint8_t *d_disp, cudaStream_t st, const PathShape &shape,
-                          cudaEvent_t ev_census, cudaEvent_t ev_end);
+                          cudaEvent_t ev_census, cudaEvent_t ev_end, KernelProbe *probe = nullptr);
 
 int set_err(sgmgb_ctx *ctx, int code, const std::string &msg);
 

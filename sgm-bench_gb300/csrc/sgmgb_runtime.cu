@@ -5,6 +5,8 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <algorithm>
+#include <vector>
 
 using namespace sgmgb;
 
@@ -101,32 +103,77 @@ static const PassSpec kPasses8[8] = {
 
 static int ms_p1(int dx, int dy) { return dy == 0 ? 40 : (dx == 0 ? 20 : 10); }
 
-static cudaError_t run_paths(const LineParams &base, int paths, int sat, bool ms, int wpb,
-                             cudaStream_t st) {
-    // passes run in order on one stream: each pair's first pass parks L in sc,
-    // its second adds it into S (the pair schedule of the 8-path sum)
+namespace {
+
+// Records an event after each launch when a probe is attached: each kernel's
+// device time, its name and its algorithmic bytes (every input byte read
+// once, every output byte written once).
+struct Marker {
+    KernelProbe *pr;
+    cudaStream_t st;
+    cudaError_t start() { return pr ? cudaEventRecord(pr->ev[0], st) : cudaSuccess; }
+    cudaError_t operator()(const char *name, double bytes) {
+        if (!pr) return cudaSuccess;
+        if (pr->n >= KernelProbe::kMax) return cudaErrorInvalidValue;
+        pr->name[pr->n] = name;
+        pr->bytes[pr->n] = bytes;
+        pr->n++;
+        return cudaEventRecord(pr->ev[pr->n], st);
+    }
+};
+
+const char *pass_name(int dx, int dy) {
+    if (dy == 0) return dx > 0 ? "path_lr" : "path_rl";
+    if (dx == 0) return dy > 0 ? "path_tb" : "path_bt";
+    if (dx > 0) return dy > 0 ? "path_diag_tl_br" : "path_diag_bl_tr";
+    return dy > 0 ? "path_diag_tr_bl" : "path_diag_br_tl";
+}
+
+double mode_bytes(int mode, double ND, double N, double Nout) {
+    switch (mode) {
+    case MODE_SCRATCH: return 2 * ND;            // C in, plane out
+    case MODE_STORE:   return 4 * ND;            // C, sc in; S out
+    case MODE_ACCUM:   return 6 * ND;            // C, sc, S in; S out
+    case MODE_FINAL:   return 4 * ND + Nout;     // C, sc, S in; disp out
+    default:           return 4 * ND + Nout;     // FINAL3: C and three planes in; disp out
+    }
+}
+
+// Passes in order on one stream: each pair's first pass parks L in sc, its
+// second adds it into S (the pair schedule of the 8-path sum).
+cudaError_t run_paths(const LineParams &base, int paths, int sat, bool ms, int wpb, cudaStream_t st,
+                      Marker &mark, double Nout) {
     const PassSpec *ps = paths == 8 ? kPasses8 : kPasses4;
+    const double ND = (double)base.W * base.H * base.D, N = (double)base.W * base.H;
     for (int i = 0; i < paths; i++) {
         LineParams p = base;
         p.dx = ps[i].dx; p.dy = ps[i].dy;
         p.p1 = ms ? ms_p1(p.dx, p.dy) : 20;
         p.nlines = lines_for(p.W, p.H, p.dx, p.dy);
         cudaError_t e = launch_line(p, ps[i].mode, sat, wpb, st);
+        if (e == cudaSuccess) e = mark(pass_name(p.dx, p.dy), mode_bytes(ps[i].mode, ND, N, Nout));
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
+}  // namespace
+
 cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8_t *d_right,
                           uint8_t *d_disp, cudaStream_t st, const PathShape &shape,
-                          cudaEvent_t ev_census, cudaEvent_t ev_end) {
+                          cudaEvent_t ev_census, cudaEvent_t ev_end, KernelProbe *probe) {
     const sgmgb_frame_desc &fd = s.fd;
     const int wpb = shape.wpb;
+    Marker mark{probe, st};
+    const double N = (double)fd.W * fd.H, ND = N * fd.D;
     cudaError_t e;
+    if ((e = mark.start()) != cudaSuccess) return e;
     if (fd.variant == SGMGB_PLAIN) {
         if ((e = launch_census2(d_left, d_right, s.cl, s.cr, fd.W, fd.H, st)) != cudaSuccess) return e;
+        if ((e = mark("census", 18 * N)) != cudaSuccess) return e;
         if ((e = launch_cost(s.cl, s.cr, s.C, nullptr, fd.W, fd.H, fd.D, kInvalidPlain, st)) != cudaSuccess)
             return e;
+        if ((e = mark("cost", 16 * N + ND)) != cudaSuccess) return e;
         if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
         LineParams p{};
         p.C = s.C; p.sc = s.sc; p.S = s.S; p.disp = d_disp;
@@ -134,55 +181,70 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         p.p2 = 192; p.even_only = 0; p.p1 = 20;
         p.key16 = (fd.paths == 4 && fd.D <= 64) ? 1 : 0;
         if (fd.paths == 8) {
-            if ((e = run_paths(p, fd.paths, 0, false, wpb, st)) != cudaSuccess) return e;
+            if ((e = run_paths(p, fd.paths, 0, false, wpb, st, mark, N)) != cudaSuccess) return e;
         } else {
             // 4 paths: R->L, B->T and L->R are independent; each parks its L in
             // a uint8 plane (the sum buffer's bytes hold planes 2 and 3) on its
-            // own stream, then T->B adds all four and takes the argmin.
+            // own stream, then T->B adds all four and takes the argmin. With a
+            // probe attached they run one after another on `st`.
             const size_t plane = (size_t)fd.W * fd.H * fd.D;
             uint8_t *pl[3] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane};
             const int dir[3][2] = {{-1, 0}, {0, -1}, {1, 0}};
-            cudaStream_t ss[3] = {st, s.aux[0], s.aux[1]};
-            if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
-            for (int k = 1; k < 3; k++)
-                if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
+            cudaStream_t ss[3] = {st, probe ? st : s.aux[0], probe ? st : s.aux[1]};
+            if (!probe) {
+                if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
+                for (int k = 1; k < 3; k++)
+                    if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
+            }
             for (int k = 0; k < 3; k++) {
                 LineParams q = p;
                 q.dx = dir[k][0]; q.dy = dir[k][1]; q.sc = pl[k];
                 q.nlines = lines_for(q.W, q.H, q.dx, q.dy);
                 if ((e = launch_line(q, MODE_SCRATCH, 0, wpb, ss[k])) != cudaSuccess) return e;
+                if ((e = mark(pass_name(q.dx, q.dy), 2 * ND)) != cudaSuccess) return e;
             }
-            for (int k = 1; k < 3; k++) {
-                if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
-                if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
+            if (!probe) {
+                for (int k = 1; k < 3; k++) {
+                    if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
+                    if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
+                }
             }
             LineParams q = p;
             q.dx = 0; q.dy = 1; q.sc = pl[0]; q.sc2 = pl[1]; q.sc3 = pl[2];
             q.nlines = lines_for(q.W, q.H, 0, 1);
             if ((e = launch_line(q, MODE_FINAL3, 0, wpb, st)) != cudaSuccess) return e;
+            if ((e = mark("path_tb_final", 4 * ND + N)) != cudaSuccess) return e;
         }
     } else {
         const int W = fd.W, H = fd.H, hw = W / 2, hh = H / 2;
+        const double Nh = (double)hw * hh, NhD = Nh * 64;
         // stage 1: half scale (multiscale/sgm_ms_ref.c:168-181)
         if ((e = launch_half2(d_left, d_right, s.halfL, s.halfR, W, H, st)) != cudaSuccess) return e;
+        if ((e = mark("half", 2 * N + 2 * Nh)) != cudaSuccess) return e;
         if ((e = launch_sobel2(s.halfL, s.halfR, s.hsobL, s.hsobR, hw, hh, st)) != cudaSuccess) return e;
+        if ((e = mark("sobel_half", 4 * Nh)) != cudaSuccess) return e;
         if ((e = launch_census2(s.hsobL, s.hsobR, s.cl1, s.cr1, hw, hh, st)) != cudaSuccess) return e;
+        if ((e = mark("census_half", 18 * Nh)) != cudaSuccess) return e;
         if ((e = launch_cost(s.cl1, s.cr1, s.C1, nullptr, hw, hh, 64, kInvalidMultiscale, st)) != cudaSuccess)
             return e;
+        if ((e = mark("cost_half", 16 * Nh + NhD)) != cudaSuccess) return e;
         if ((e = launch_sobel2(d_left, d_right, s.sobL, s.sobR, W, H, st)) != cudaSuccess) return e;
+        if ((e = mark("sobel", 4 * N)) != cudaSuccess) return e;
         if ((e = launch_census2(s.sobL, s.sobR, s.cl, s.cr, W, H, st)) != cudaSuccess) return e;
+        if ((e = mark("census", 18 * N)) != cudaSuccess) return e;
         if ((e = launch_cost(s.cl, s.cr, s.C, s.C1, W, H, 64, kInvalidMultiscale, st)) != cudaSuccess)
             return e;
+        if ((e = mark("cost_merge", 16 * N + NhD + ND)) != cudaSuccess) return e;
         if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
         LineParams p1{};
         p1.C = s.C1; p1.sc = s.sc; p1.S = s.S; p1.disp = s.disp1;
         p1.W = hw; p1.H = hh; p1.D = 64; p1.dpl = shape.dpl; p1.p2 = 200; p1.even_only = 0;
-        if ((e = run_paths(p1, 8, 1, true, wpb, st)) != cudaSuccess) return e;
+        if ((e = run_paths(p1, 8, 1, true, wpb, st, mark, Nh)) != cudaSuccess) return e;
         // stage 2: full scale, cost averaged with the half-scale cost (:183-199)
         LineParams p2{};
         p2.C = s.C; p2.sc = s.sc; p2.S = s.S; p2.disp = d_disp;
         p2.W = W; p2.H = H; p2.D = 64; p2.dpl = shape.dpl; p2.p2 = 200; p2.even_only = 1;
-        if ((e = run_paths(p2, 8, 1, true, wpb, st)) != cudaSuccess) return e;
+        if ((e = run_paths(p2, 8, 1, true, wpb, st, mark, Nh)) != cudaSuccess) return e;
     }
     if (ev_end && (e = cudaEventRecord(ev_end, st)) != cudaSuccess) return e;
     return cudaSuccess;
@@ -196,6 +258,7 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
 extern "C" {
 
 static void drop_graph(sgmgb_ctx *ctx);
+static int cuda_fail(sgmgb_ctx *ctx, cudaError_t e, const char *what);
 
 int sgmgb_abi_version(void) { return SGMGB_ABI_VERSION; }
 
@@ -267,6 +330,39 @@ int sgmgb_create(int device, sgmgb_ctx **out) {
         return SGMGB_ERR_CUDA;
     }
     *out = ctx;
+    return SGMGB_OK;
+}
+
+int sgmgb_profile_frame(sgmgb_ctx *ctx, const uint8_t *d_left, const uint8_t *d_right, uint8_t *d_disp,
+                        int reps, sgmgb_kernel_stat *out, int max_out, int *n_out) {
+    if (!ctx || !d_left || !d_right || !d_disp || reps < 1 || !out || max_out < 1 || !n_out) return SGMGB_ERR_ARG;
+    if (!ctx->planned) return set_err(ctx, SGMGB_ERR_STATE, "sgmgb_plan has not been called");
+    cudaSetDevice(ctx->device);
+    KernelProbe pr;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i <= KernelProbe::kMax && e == cudaSuccess; i++) e = cudaEventCreate(&pr.ev[i]);
+    std::vector<double> sum(KernelProbe::kMax, 0.0);
+    int n = 0;
+    for (int r = 0; r < reps && e == cudaSuccess; r++) {
+        pr.n = 0;
+        e = enqueue_frame(*ctx->slot, d_left, d_right, d_disp, ctx->stream, ctx->shape, nullptr, nullptr, &pr);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        for (int k = 0; k < pr.n && e == cudaSuccess; k++) {
+            float ms = 0.f;
+            e = cudaEventElapsedTime(&ms, pr.ev[k], pr.ev[k + 1]);
+            sum[k] += ms;
+        }
+        n = pr.n;
+    }
+    for (int i = 0; i <= KernelProbe::kMax; i++) if (pr.ev[i]) cudaEventDestroy(pr.ev[i]);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "profile_frame");
+    *n_out = std::min(n, max_out);
+    for (int k = 0; k < *n_out; k++) {
+        memset(out[k].name, 0, sizeof out[k].name);
+        strncpy(out[k].name, pr.name[k], sizeof out[k].name - 1);
+        out[k].ms = sum[k] / reps;
+        out[k].bytes = pr.bytes[k];
+    }
     return SGMGB_OK;
 }
 

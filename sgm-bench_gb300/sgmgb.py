@@ -26,6 +26,7 @@ OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_NODEV, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE 
 EXPORTS = [
     "sgmgb_abi_version", "sgmgb_strerror", "sgmgb_last_error", "sgmgb_check_desc", "sgmgb_out_size",
     "sgmgb_workspace_bytes", "sgmgb_create", "sgmgb_destroy", "sgmgb_plan", "sgmgb_set_path_shape",
+    "sgmgb_profile_frame",
     "sgmgb_run_frame",
     "sgmgb_run_frame_async", "sgmgb_sync", "sgmgb_census_async", "sgmgb_batch_create", "sgmgb_batch_run",
     "sgmgb_batch_wait", "sgmgb_batch_autotune", "sgmgb_batch_tile_shape", "sgmgb_batch_set_fault",
@@ -47,6 +48,10 @@ class StageTimes(ctypes.Structure):
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 24), ("ms", ctypes.c_double), ("bytes", ctypes.c_double)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -83,6 +88,7 @@ def _load():
         "sgmgb_destroy": (None, [vp]),
         "sgmgb_plan": (i, [vp, fdp]),
         "sgmgb_set_path_shape": (i, [vp, i, i]),
+        "sgmgb_profile_frame": (i, [vp, u8p, u8p, u8p, i, ctypes.POINTER(KernelStat), i, ctypes.POINTER(i)]),
         "sgmgb_run_frame": (i, [vp, u8p, u8p, u8p, ctypes.POINTER(StageTimes)]),
         "sgmgb_run_frame_async": (i, [vp, u8p, u8p, u8p, vp]),
         "sgmgb_sync": (i, [vp, vp]),
@@ -225,6 +231,15 @@ class Engine:
         """Path-kernel shape (speed only; results are identical)."""
         self._check(lib.sgmgb_set_path_shape(self.h, warps_per_block, disp_per_lane))
         return self
+
+    def profile_frame(self, d_left, d_right, d_disp, reps=10):
+        """Per-kernel mean device time (ms) and algorithmic bytes of the planned
+        frame, every kernel timed alone with CUDA events: [(name, ms, bytes)]."""
+        out = (KernelStat * 32)()
+        n = ctypes.c_int()
+        self._check(lib.sgmgb_profile_frame(self.h, _ptr(d_left), _ptr(d_right), _ptr(d_disp), reps, out, 32,
+                                            ctypes.byref(n)))
+        return [(out[k].name.decode(), out[k].ms, out[k].bytes) for k in range(n.value)]
 
     def run_frame(self, left, right, times=False):
         """Host arrays in, host disparity map out (the drop-in call)."""

@@ -193,3 +193,23 @@ def test_config_a_full_size_async(engine):
     assert np.array_equal(dd.cpu().numpy(), want)
     # host path gives the same bytes
     assert np.array_equal(engine.run_frame(left, right), want)
+
+
+def test_profile_frame_lists_every_kernel(engine):
+    import torch
+    W, H = 320, 200
+    left, right, _ = sgmgb.synth_pair(W, H, 64, seed=3)
+    dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
+    dd = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+    engine.plan(W, H, 64, 4)
+    stats = engine.profile_frame(dl, dr, dd, reps=3)
+    assert [s[0] for s in stats] == ["census", "cost", "path_rl", "path_bt", "path_lr", "path_tb_final"]
+    assert all(ms > 0 and b > 0 for _, ms, b in stats)
+    assert stats[-1][2] == 4 * W * H * 64 + W * H
+    assert np.array_equal(dd.cpu().numpy(), oracle.plain(left, right, 64, 4))   # the timed frames are real frames
+    engine.plan(W, H, 64, 8, sgmgb.MULTISCALE)
+    dd2 = torch.zeros((H // 2, W // 2), dtype=torch.uint8, device="cuda")
+    names = [s[0] for s in engine.profile_frame(dl, dr, dd2, reps=2)]
+    assert names[:7] == ["half", "sobel_half", "census_half", "cost_half", "sobel", "census", "cost_merge"]
+    assert len(names) == 7 + 16
+    assert np.array_equal(dd2.cpu().numpy(), oracle.multiscale(left, right))
