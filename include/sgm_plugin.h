@@ -22,8 +22,8 @@ extern "C" {
 
 /* Same fields, order and types as common/sgm.h:9-25. */
 typedef struct {
-    double census_ms;
-    double cost_ms;       /* -1: the cost is fused into aggregation here */
+    double census_ms;     /* census and the cost volume */
+    double cost_ms;       /* -1: timed with the census (census_ms covers both) */
     double aggregate_ms;
     double argmin_ms;     /* -1: the argmin is fused into the last path pass */
     double transfer_ms;   /* host<->device copies, kept apart from the phases */

@@ -20,8 +20,9 @@
  *                         sgm_gb300.c wraps it as SGM_IMPL.
  *   sgmgb_run_frame_async the device half of cuda_run (cuda/sgm_cuda_opt.cu:
  *                         321-366): inputs already on the device, one stream.
- *   sgmgb_ms_run          the standalone multi-scale binary's frame loop
- *                         (multiscale/sgm_ms_ref.c:166-202).
+ *   SGMGB_MULTISCALE plans the frame loop of the standalone multi-scale
+ *                         binary (multiscale/sgm_ms_ref.c:166-202).
+ *   sgmgb_profile_frame   no reference symbol: per-kernel timing for the bench.
  *   sgmgb_batch_*         no reference symbol: many frames per launch.
  *   sgmgb_server_*        no reference symbol: a continuous-batching request loop.
  */

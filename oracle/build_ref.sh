@@ -6,6 +6,8 @@
 #   sgm_ref_d{64,128,256}_p{4,8}  common/sgm_ref.c + harness.c + util.c (Makefile:40-41 flags)
 #   sgm_ms_ref                    multiscale/sgm_ms_ref.c + util.c (OpenMP)
 #   gen_synthetic_d{64,128,256}   common/gen_synthetic.c
+#   sgm_gb300_harness_d64_p4      the reference's harness.c + util.c linked against this
+#                                 engine's sgm.h plugin (when it is built): the drop-in link
 set -eu
 REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -21,4 +23,9 @@ for D in 64 128 256; do
   gcc -O2 -Wall -I"$REF/common" -DSGM_D=$D -o "$OUT/gen_synthetic_d$D" "$REF/common/gen_synthetic.c" -lm
 done
 gcc -O2 -Wall -std=gnu11 -fopenmp -I"$REF/common" -o "$OUT/sgm_ms_ref" "$REF/multiscale/sgm_ms_ref.c" "$REF/common/util.c" -lm
+PLUG="$HERE/../sgm-bench_gb300/_build"
+if [ -f "$PLUG/libsgm_gb300_d64_p4.so" ]; then
+  gcc $CFLAGS -DGIT_SHA='"gb300"' -DCFLAGS_STR='"gb300 sm_103a"' -o "$OUT/sgm_gb300_harness_d64_p4" \
+      "$REF/common/harness.c" "$REF/common/util.c" -L"$PLUG" -lsgm_gb300_d64_p4 -Wl,-rpath,"$PLUG" -lm
+fi
 echo "$OUT"

@@ -75,3 +75,30 @@ def test_multiscale_matches_reference_binary(tmp_path, W, H):
                     "-o", str(tmp_path / "o.pgm")], check=True, capture_output=True,
                    env=dict(os.environ, OMP_NUM_THREADS="2"))
     assert np.array_equal(read_pgm(str(tmp_path / "o.pgm")), oracle.multiscale(l, r))
+
+
+def test_reference_harness_links_the_plugin(tmp_path):
+    """The reference's own harness.c, linked against the gb300 SGM_IMPL: on a
+    machine without a GPU it must fail the frame cleanly (exit 1, "impl
+    failed"), on a GPU it must pass the golden-style comparison."""
+    exe = os.path.join(REF, "sgm_gb300_harness_d64_p4")
+    if not os.path.exists(exe):
+        pytest.skip("plugin harness not linked")
+    rng = np.random.default_rng(4)
+    l = rng.integers(0, 256, (48, 64), dtype=np.uint8)
+    r = rng.integers(0, 256, (48, 64), dtype=np.uint8)
+    write_pgm(str(tmp_path / "l.pgm"), l)
+    write_pgm(str(tmp_path / "r.pgm"), r)
+    want = oracle.plain(l, r, 64, 4)
+    write_pgm(str(tmp_path / "g.pgm"), want)
+    p = subprocess.run([exe, str(tmp_path / "l.pgm"), str(tmp_path / "r.pgm"), "-g", str(tmp_path / "g.pgm"),
+                        "-w", "0", "-n", "1"], capture_output=True, text=True)
+    try:
+        import torch
+        gpu = torch.cuda.is_available()
+    except Exception:
+        gpu = False
+    if gpu:
+        assert p.returncode == 0, p.stdout + p.stderr
+    else:
+        assert p.returncode == 1 and "impl failed" in (p.stdout + p.stderr)
