@@ -33,6 +33,7 @@ EXPORTS = [
     "sgmgb_batch_destroy", "sgmgb_tune_lookup", "sgmgb_tune_record",
     "sgmgb_server_create", "sgmgb_server_add_camera", "sgmgb_server_submit", "sgmgb_server_poll",
     "sgmgb_server_wait", "sgmgb_server_stats_get", "sgmgb_server_destroy", "sgmgb_synth_pair",
+    "sgmgb_run_frame_noalloc",
 ]
 
 
@@ -111,6 +112,7 @@ def _load():
         "sgmgb_server_stats_get": (i, [vp, ctypes.POINTER(ServerStats)]),
         "sgmgb_server_destroy": (None, [vp]),
         "sgmgb_synth_pair": (i, [i, i, i, ctypes.c_uint64, u8p, u8p, u8p]),
+        "sgmgb_run_frame_noalloc": (i, [u8p, u8p, u8p, i, i, i, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
