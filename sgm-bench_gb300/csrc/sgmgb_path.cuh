@@ -19,10 +19,11 @@
 // with a = prev[d] <= 255 in the minimum,
 //   min(a, sat(lo+P1), sat(hi+P1), sat(mn+P2)) == min(a, lo+P1, hi+P1, mn+P2)
 // because any term that would saturate is >= 255 >= a (common/sgm_ref.c:61-72).
-// The per-step minimum over d is one group-masked warp REDUX of a packed value
-// (v | v << 16), so the result is already the packed pair the next step needs.
-// Lanes past the last disparity carry cost 0x3FFF, so they never win a
-// minimum. The multi-scale variant clamps L to 255 (multiscale/sgm_ms_ref.c:82).
+// The per-step minimum over d is a warp REDUX of a packed value (v | v << 16)
+// per lane group (group_min), so the result is already the packed pair the
+// next step needs. Lanes past the last disparity never win a minimum (see the
+// ring fill below). The multi-scale variant clamps L to 255
+// (multiscale/sgm_ms_ref.c:82).
 // The first pixel of a line needs no special case: with L_prev = 0 and
 // min_prev = 0 the recurrence gives L = C, which is the reference's start.
 //
@@ -65,6 +66,27 @@ __device__ __forceinline__ void cp_async16(uint32_t dst_smem, const void *src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Minimum of v over this lane's group of lines (G groups of 32/G lanes; g is
+// the lane's group, gmask its lanes). For G <= 4 it takes G full-warp
+// reductions, each group's lanes contributing and the others passing ~0:
+// one reduction per distinct member mask in flight at a time, which keeps the
+// warp converged; larger G uses the group-masked form.
+__device__ __forceinline__ uint32_t group_min(uint32_t v, int G, int g, uint32_t gmask) {
+    if (G == 1) return __reduce_min_sync(kFull, v);
+    if (G <= 4) {
+        uint32_t r = __reduce_min_sync(kFull, g == 0 ? v : kFull);
+        const uint32_t r1 = __reduce_min_sync(kFull, g == 1 ? v : kFull);
+        r = g == 1 ? r1 : r;
+        if (G == 4) {
+            const uint32_t r2 = __reduce_min_sync(kFull, g == 2 ? v : kFull);
+            const uint32_t r3 = __reduce_min_sync(kFull, g == 3 ? v : kFull);
+            r = g == 2 ? r2 : (g == 3 ? r3 : r);
+        }
+        return r;
+    }
+    return __reduce_min_sync(gmask, v);
+}
 
 template <int MODE> struct Planes {   // scratch planes a pass reads
     static constexpr int N = MODE == MODE_SCRATCH ? 0 : (MODE == MODE_FINAL3 ? 3 : 1);
@@ -154,9 +176,9 @@ __device__ __forceinline__ uint32_t byte_pair(const uint32_t *w, int i) {
 // pixel at this step; `lead`: the group's first lane; `gmask`: the group.
 // `out` points at this lane's bytes of pixel p in sc (SCRATCH) or S (STORE,
 // ACCUM). KEY16: the argmin key S*64 + d fits a packed u16 (4 paths, D <= 64).
-template <int DPL, int MODE, bool KEY16>
+template <int DPL, int MODE, bool KEY16, bool ONE>
 __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int x, int y, int d0,
-                                     bool lead, uint32_t gmask, bool live, const uint32_t (&L)[DPL / 2],
+                                     bool lead, int g, uint32_t gmask, bool live, const uint32_t (&L)[DPL / 2],
                                      const StepIn<DPL, MODE> &s) {
     constexpr int NR = DPL / 2;
     constexpr int SCW = StepIn<DPL, MODE>::SCW;
@@ -190,8 +212,10 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
         else *(uint4 *)sp = make_uint4(tot[0], tot[1], tot[2], tot[3]);
         return;
     }
-    // final passes: argmin over d, the lowest d winning ties
-    if (MODE == MODE_FINAL && P.even_only && ((x | y) & 1)) return;   // uniform within the group
+    // final passes: argmin over d, the lowest d winning ties. Every lane of the
+    // warp reaches group_min (it may reduce over the whole warp); a pixel that
+    // is not kept (odd x or y of an even-only map) only skips the store.
+    const bool keep = live && !(MODE == MODE_FINAL && P.even_only && ((x | y) & 1));
     uint32_t key;
     if (KEY16) {
         uint32_t k = kFull;
@@ -208,8 +232,8 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
             }
         }
     }
-    key = __reduce_min_sync(gmask, key);
-    if (lead && live) {
+    key = ONE ? __reduce_min_sync(kFull, key) : group_min(key, P.gpw, g, gmask);
+    if (lead && keep) {
         const uint8_t d = (uint8_t)(KEY16 ? (key & 0x3Fu) : (key & 0xFFu));
         if (MODE == MODE_FINAL && P.even_only) P.disp[(size_t)(y >> 1) * (P.W >> 1) + (x >> 1)] = d;
         else P.disp[p] = d;
@@ -362,9 +386,11 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
     if (MODE != MODE_FINAL && MODE != MODE_FINAL3) out -= out_step;
 
     // One recurrence step on the next pixel of the line; FULL: every line of
-    // the warp has this pixel (no per-step length test).
-    auto step_once = [&](const In &s, int i, auto full_t) {
+    // the warp has this pixel (no per-step length test); ONE: the warp holds
+    // one line (a plain full-warp reduction).
+    auto step_once = [&](const In &s, int i, auto full_t, auto one_t) {
         constexpr bool FULL = decltype(full_t)::value;
+        constexpr bool ONE = decltype(one_t)::value;
         x += dx; y += dy; p += step;
         if (MODE != MODE_FINAL && MODE != MODE_FINAL3) out += out_step;
         const bool live = FULL ? active : i < len;
@@ -390,26 +416,31 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
             L[j] = v;
             tm = vmin2(tm, v);
         }
-        mn = __reduce_min_sync(gmask, fold2(tm));
-        emit<DPL, MODE, KEY16>(P, out, p, x, y, d0, lead, gmask, live, L, s);
+        mn = ONE ? __reduce_min_sync(kFull, fold2(tm)) : group_min(fold2(tm), G, g, gmask);
+        emit<DPL, MODE, KEY16, ONE>(P, out, p, x, y, d0, lead, g, gmask, live, L, s);
     };
 
-    for (int ch = 0; ch < nchunks; ch++) {
-        cp_async_wait<NCH - 2>();   // chunk ch has landed (this lane's copies)
-        __syncwarp();               // ... and every lane's; slot ch-1 is free
-        issue(ch + NCH - 1);
-        const uint8_t *chunk = ring + (ch % NCH) * SLOT;
-        In s[K];                    // the chunk's inputs, read before its steps run
+    // the chunk loop, instantiated for one line per warp and for several
+    auto run = [&](auto one_t) {
+        for (int ch = 0; ch < nchunks; ch++) {
+            cp_async_wait<NCH - 2>();   // chunk ch has landed (this lane's copies)
+            __syncwarp();               // ... and every lane's; slot ch-1 is free
+            issue(ch + NCH - 1);
+            const uint8_t *chunk = ring + (ch % NCH) * SLOT;
+            In s[K];                    // the chunk's inputs, read before its steps run
 #pragma unroll
-        for (int k = 0; k < K; k++) ring_read<DPL, MODE>(chunk, lane, k, s[k]);
-        if ((ch + 1) * K <= minlen) {
+            for (int k = 0; k < K; k++) ring_read<DPL, MODE>(chunk, lane, k, s[k]);
+            if ((ch + 1) * K <= minlen) {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(s[k], ch * K + k, std::true_type{});
-        } else {
+                for (int k = 0; k < K; k++) step_once(s[k], ch * K + k, std::true_type{}, one_t);
+            } else {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(s[k], ch * K + k, std::false_type{});
+                for (int k = 0; k < K; k++) step_once(s[k], ch * K + k, std::false_type{}, one_t);
+            }
         }
-    }
+    };
+    if (G == 1) run(std::true_type{});
+    else run(std::false_type{});
     cp_async_wait<0>();   // no copy outlives the kernel
 }
 
