@@ -1,7 +1,7 @@
 // sgmgb_batch.cu -- many frames of mixed sizes in one persistent launch.
 //
 // Work decomposition (plain variant, common/sgm_ref.c semantics per frame):
-//   phase 0  census   one item per band of BAND rows (both images)
+//   phase 0  census   one item per band of BAND (8) rows (both images)
 //   phase 1  cost     one item per band: C[p][d] from the band's census rows
 //   4 paths: phase 2  R->L, B->T, L->R into three u8 planes (all three passes)
 //            phase 3  T->B adds the planes to its L and takes the argmin
@@ -16,6 +16,7 @@
 // (cp.async.cg, ld.global.cg): a block never reads such data through its L1.
 #include "sgmgb_internal.h"
 #include "sgmgb_path.cuh"
+#include "sgmgb_tiles.cuh"
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -26,8 +27,7 @@ namespace sgmgb {
 
 namespace {
 
-constexpr int BAND = 4;          // rows per census / cost item
-constexpr int TX = 64;           // columns per census / cost tile
+constexpr int BAND = tiles::CEN_ROWS;   // rows per census / cost item
 constexpr int MAXPH = 10;        // phases per frame (8 paths: census, cost, 8 passes)
 
 enum ItemKind : int { IT_CENSUS = 0, IT_COST = 1, IT_PATH = 2 };
@@ -87,84 +87,25 @@ __device__ bool wait_count(const unsigned *cnt, unsigned need, BCtl *ctl, int it
     }
 }
 
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // Census 9x7 of rows [y0, y0+BAND) of both images (common/sgm_ref.c:23-41),
-// staged through shared memory one TX-column tile at a time.
+// one 128-pixel tile at a time (sgmgb_tiles.cuh).
 __device__ void item_census(const BFrame &F, int band, uint8_t *sm) {
-    const int W = F.W, H = F.H, y0 = band * BAND, nt = blockDim.x;
-    constexpr int TW = TX + 8, TH = BAND + 6;
-    for (int img = 0; img < 2; img++) {
-        const uint8_t *im = img ? F.right : F.left;
-        uint64_t *out = img ? F.cr : F.cl;
-        for (int x0 = 0; x0 < W; x0 += TX) {
-            for (int i = threadIdx.x; i < TW * TH; i += nt) {
-                const int ty = i / TW, tx = i - ty * TW;
-                sm[i] = __ldg(im + (size_t)clampi(y0 + ty - 3, 0, H - 1) * W + clampi(x0 + tx - 4, 0, W - 1));
-            }
-            __syncthreads();
-            for (int i = threadIdx.x; i < TX * BAND; i += nt) {
-                const int ty = i / TX, tx = i - ty * TX, x = x0 + tx, y = y0 + ty;
-                if (x < W && y < H) {
-                    const uint8_t *c = sm + (ty + 3) * TW + (tx + 4);
-                    const uint32_t cv = *c;
-                    uint64_t bits = 0;
-                    int n = 0;
-#pragma unroll
-                    for (int dy = -3; dy <= 3; dy++)
-#pragma unroll
-                        for (int dx = -4; dx <= 4; dx++) {
-                            if (dx == 0 && dy == 0) continue;
-                            bits |= (uint64_t)(c[dy * TW + dx] < cv) << n;
-                            n++;
-                        }
-                    out[(size_t)y * W + x] = bits;
-                }
-            }
-            __syncthreads();
-        }
-    }
+    for (int img = 0; img < 2; img++)
+        for (int x0 = 0; x0 < F.W; x0 += tiles::CEN_PX)
+            tiles::census_tile(img ? F.right : F.left, img ? F.cr : F.cl, F.W, F.H, x0, band * BAND, sm,
+                               threadIdx.x, blockDim.x);
 }
 
 // Cost C[(y*W + x)*D + d] = popcount(cl[x] ^ cr[x-d]), 62 where x - d < 0
-// (common/sgm_ref.c:44-56), for rows [y0, y0+BAND). Per TX-column tile the
-// left descriptors and the right ones from D-1 columns before the tile are
-// staged in shared memory; each thread makes 8 disparities of one pixel.
-__device__ void item_cost(const BFrame &F, int band, uint8_t *smb) {
-    const int W = F.W, H = F.H, D = F.D, y0 = band * BAND, nt = blockDim.x;
-    uint64_t *sl = (uint64_t *)smb;         // TX left descriptors
-    uint64_t *sr = sl + TX;                 // D-1+TX right descriptors, sr[j] = cr[x0 - (D-1) + j]
-    const int tpp = D >> 3;                 // threads per pixel
-    for (int y = y0; y < min(y0 + BAND, H); y++) {
-        const uint64_t *cl = F.cl + (size_t)y * W, *cr = F.cr + (size_t)y * W;
-        for (int x0 = 0; x0 < W; x0 += TX) {
-            for (int i = threadIdx.x; i < TX + D - 1 + TX; i += nt) {
-                if (i < TX) {
-                    sl[i] = x0 + i < W ? __ldcg(cl + x0 + i) : 0;
-                } else {
-                    const int j = i - TX, x = x0 - (D - 1) + j;
-                    sr[j] = (x >= 0 && x < W) ? __ldcg(cr + x) : 0;
-                }
-            }
-            __syncthreads();
-            for (int t = threadIdx.x; t < TX * tpp; t += nt) {
-                const int px = t / tpp, d0 = (t - px * tpp) * 8, x = x0 + px;
-                if (x < W) {
-                    const uint64_t a = sl[px];
-                    uint32_t v[8];
-#pragma unroll
-                    for (int k = 0; k < 8; k++) {
-                        const int d = d0 + k;
-                        v[k] = x - d >= 0 ? (uint32_t)__popcll(a ^ sr[px + (D - 1) - d]) : (uint32_t)kInvalidPlain;
-                    }
-                    const uint32_t lo = v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24);
-                    const uint32_t hi = v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24);
-                    *(uint2 *)(F.C + ((size_t)y * W + x) * D + d0) = make_uint2(lo, hi);
-                }
-            }
-            __syncthreads();
-        }
-    }
+// (common/sgm_ref.c:44-56), for rows [y0, y0+BAND), one 64-pixel tile at a
+// time; the descriptors were written by other blocks, so they are read
+// through L2 only.
+__device__ void item_cost(const BFrame &F, int band, uint8_t *sm) {
+    for (int y = band * BAND; y < min(band * BAND + BAND, F.H); y++)
+        for (int x0 = 0; x0 < F.W; x0 += tiles::COST_PX)
+            tiles::cost_tile<true>(F.cl, F.cr, F.C, nullptr, F.W, F.D, kInvalidPlain, y, x0, sm, threadIdx.x,
+                                   blockDim.x);
 }
 
 // One warp's share of a path item: lines of warp `warp` of pass `bp`.
@@ -375,9 +316,9 @@ int build_plan(sgmgb_batch *b) {
     b->n_items = (int)items.size();
     b->n_passes = (int)passes.size();
     b->ring_bytes = ring;
-    // census tile (72 x 10 bytes) and cost tile (2*TX + D - 1 descriptors) fit in any ring
+    // the census and cost tiles reuse the start of the block's path rings
     size_t smem = (size_t)ring * b->wpb;
-    smem = std::max(smem, (size_t)(2 * TX + 256) * 8);
+    smem = std::max(smem, (size_t)std::max(tiles::CEN_SMEM, tiles::COST_SMEM));
     b->smem_bytes = smem;
     // one device allocation for all tables
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };

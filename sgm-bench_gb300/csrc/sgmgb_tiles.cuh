@@ -1,0 +1,176 @@
+// sgmgb_tiles.cuh -- census and cost of one tile, shared by the per-frame
+// kernels (sgmgb_kernels.cu) and the persistent batch kernel (sgmgb_batch.cu).
+// Both functions are called by every thread of a block (they synchronise it).
+#pragma once
+#include <cstdint>
+#include "sgmgb_kernels.cuh"
+
+namespace sgmgb {
+namespace tiles {
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// ---------------------------------------------------------------------------
+// Census 9x7 (common/sgm_ref.c:23-41): bit n is set iff the neighbour is
+// darker than the centre, n running over dy (outer) then dx, skipping the
+// centre, with clamped (edge-replicated) coordinates.
+//
+// A thread makes 4 horizontally adjacent pixels with 4-byte SIMD-within-a-
+// register compares: for one (dx, dy) offset the 4 neighbour bytes and the 4
+// centre bytes are compared at once by a borrow-free per-byte "less than"
+// (result in each byte's top bit), and 8 offsets in a row are gathered into
+// one word per 8 census bits (byte i = pixel i) by shifting right and OR-ing
+// the top bits in. A byte transpose at the end gives each pixel's 62-bit
+// descriptor. A tile is CEN_PX x CEN_ROWS pixels plus its 4/3-pixel halo,
+// staged in shared memory.
+// ---------------------------------------------------------------------------
+constexpr int CEN_PX = 128, CEN_ROWS = 8, CEN_TW = CEN_PX + 8, CEN_TH = CEN_ROWS + 6;
+constexpr int CEN_SMEM = CEN_TW * CEN_TH;            // bytes, 16-byte aligned by the caller
+
+__device__ __forceinline__ uint32_t bytes_lt(uint32_t n, uint32_t c, uint32_t c7) {
+    // per byte: n < c, in the byte's top bit (the other bits are garbage)
+    const uint32_t t = (n | 0x80808080u) - c7;       // top bit of a byte: (n & 0x7f) >= (c & 0x7f)
+    return (~n & c) | (~(n ^ c) & ~t);
+}
+
+// bytes s..s+3 of the 12-byte run w0:w1:w2
+__device__ __forceinline__ uint32_t window4(uint32_t w0, uint32_t w1, uint32_t w2, int s) {
+    if (s == 0) return w0;
+    if (s == 4) return w1;
+    if (s == 8) return w2;
+    const uint32_t sel = (s & 3) | (((s & 3) + 1) << 4) | (((s & 3) + 2) << 8) | (((s & 3) + 3) << 12);
+    return s < 4 ? __byte_perm(w0, w1, sel) : __byte_perm(w1, w2, sel);
+}
+
+// Census of the tile at (x0, y0) of one W x H image into out (W*H uint64).
+// nthreads: a multiple of 32; tid in [0, nthreads). ld_cg: read the image
+// through L2 only (it may have been written by another block of this launch).
+__device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint64_t *__restrict__ out,
+                                            int W, int H, int x0, int y0, uint8_t *smem, int tid,
+                                            int nthreads) {
+    uint32_t *tile = (uint32_t *)smem;                // [CEN_TH][CEN_TW / 4]
+    for (int i = tid; i < CEN_SMEM; i += nthreads) {
+        const int ty = i / CEN_TW, tx = i - ty * CEN_TW;
+        smem[i] = __ldg(im + (size_t)clampi(y0 + ty - 3, 0, H - 1) * W + clampi(x0 + tx - 4, 0, W - 1));
+    }
+    __syncthreads();
+    constexpr int RW = CEN_TW / 4;                    // words per tile row
+    for (int job = tid; job < 32 * CEN_ROWS; job += nthreads) {
+        const int tx = job & 31, ty = job >> 5;
+        const int x = x0 + 4 * tx, y = y0 + ty;
+        if (x >= W || y >= H) continue;
+        const uint32_t c = tile[(ty + 3) * RW + tx + 1], c7 = c & 0x7F7F7F7Fu;
+        uint32_t A[8];
+        uint32_t acc = 0;
+        int n = 0;
+#pragma unroll
+        for (int dy = -3; dy <= 3; dy++) {
+            const uint32_t *r = tile + (ty + 3 + dy) * RW + tx;
+            const uint32_t w0 = r[0], w1 = r[1], w2 = r[2];
+#pragma unroll
+            for (int dx = -4; dx <= 4; dx++) {
+                if (dx == 0 && dy == 0) continue;
+                acc = (acc >> 1) | (bytes_lt(window4(w0, w1, w2, 4 + dx), c, c7) & 0x80808080u);
+                if ((++n & 7) == 0) { A[(n >> 3) - 1] = acc; acc = 0; }
+            }
+        }
+        A[7] = acc >> 2;                              // bits 56..61: six compares, aligned to bit 0
+        uint64_t d[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t sel = i | ((i + 4) << 4);
+            const uint32_t lo = __byte_perm(__byte_perm(A[0], A[1], sel), __byte_perm(A[2], A[3], sel), 0x5410);
+            const uint32_t hi = __byte_perm(__byte_perm(A[4], A[5], sel), __byte_perm(A[6], A[7], sel), 0x5410);
+            d[i] = ((uint64_t)hi << 32) | lo;
+        }
+        uint64_t *o = out + (size_t)y * W + x;
+        if (x + 3 < W) {
+            if ((((size_t)y * W + x) & 1) == 0) {
+                ((ulonglong2 *)o)[0] = make_ulonglong2(d[0], d[1]);
+                ((ulonglong2 *)o)[1] = make_ulonglong2(d[2], d[3]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; i++) o[i] = d[i];
+            }
+        } else {
+            for (int i = 0; i < 4 && x + i < W; i++) o[i] = d[i];
+        }
+    }
+    __syncthreads();                                  // the tile memory may be reused next
+}
+
+// ---------------------------------------------------------------------------
+// Cost C[(y*W + x)*D + d], uint8, of COST_PX pixels of row y from x0:
+//   plain:        popcount(cl[x] ^ cr[x-d]), `invalid` (62) where x-d < 0   (common/sgm_ref.c:44-56)
+//   half scale:   the same with 63                                       (multiscale/sgm_ms_ref.c:66-72)
+//   full scale:   (own cost, 63 invalid) averaged with the half-scale cost
+//                 at (x/2, y/2, d/2): (c2 + c1 + 1) >> 1                 (multiscale/sgm_ms_ref.c:184-188)
+// The row's left descriptors and the right ones from D-1 columns before the
+// tile are staged in shared memory. A thread makes 8 consecutive disparities
+// of one pixel and stores them as one 8-byte word. A warp covers 8 pixels x 4
+// disparity groups (16 x 2 when D/8 is not a multiple of 4): its 32 right-
+// descriptor reads for one k are then 32 consecutive words (no bank
+// conflicts), and each pixel's 32 bytes of the warp are one sector in the
+// store. The population counts (2 POPC per cost) are the bound.
+// ---------------------------------------------------------------------------
+constexpr int COST_PX = 64;
+constexpr int COST_SMEM = (COST_PX + COST_PX + 256) * 8;   // bytes, 16-byte aligned by the caller
+
+template <bool LD_CG>
+__device__ __forceinline__ uint64_t ld_desc(const uint64_t *p) {
+    return LD_CG ? __ldcg(p) : __ldg(p);
+}
+
+template <bool LD_CG>
+__device__ __forceinline__ void cost_tile(const uint64_t *__restrict__ cl, const uint64_t *__restrict__ cr,
+                                          uint8_t *__restrict__ C, const uint8_t *__restrict__ C1, int W,
+                                          int D, int invalid, int y, int x0, uint8_t *smem, int tid,
+                                          int nthreads) {
+    uint64_t *sl = (uint64_t *)smem;                  // COST_PX left descriptors
+    uint64_t *sr = sl + COST_PX;                      // sr[j] = cr[x0 - (D-1) + j]
+    const uint64_t *rl = cl + (size_t)y * W, *rr = cr + (size_t)y * W;
+    const int nr = COST_PX + D - 1;
+    for (int i = tid; i < COST_PX + nr; i += nthreads) {
+        if (i < COST_PX) {
+            sl[i] = x0 + i < W ? ld_desc<LD_CG>(rl + x0 + i) : 0ull;
+        } else {
+            const int j = i - COST_PX, x = x0 - (D - 1) + j;
+            sr[j] = (x >= 0 && x < W) ? ld_desc<LD_CG>(rr + x) : 0ull;
+        }
+    }
+    __syncthreads();
+    const int tpp = D >> 3;                           // disparity groups of 8 per pixel
+    const int DG = (tpp & 3) ? 2 : 4, PXW = 32 / DG;
+    const int lane = tid & 31;
+    const int pxl = DG == 4 ? lane >> 2 : lane >> 1, dgl = lane & (DG - 1);
+    const int nxb = COST_PX / PXW, ntask = nxb * (tpp / DG);
+    const int hw = W >> 1;
+    uint8_t *row = C + (size_t)y * W * D;
+    for (int task = tid >> 5; task < ntask; task += nthreads >> 5) {
+        const int dgb = task / nxb, px = (task - dgb * nxb) * PXW + pxl;
+        const int d0 = (dgb * DG + dgl) * 8, x = x0 + px;
+        if (x >= W) continue;
+        const uint64_t a = sl[px];
+        const uint64_t *r = sr + px + (D - 1) - d0;   // r[-k] = cr[x - d0 - k]
+        uint32_t v[8];
+        if (x >= d0 + 7) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = (uint32_t)__popcll(a ^ r[-k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = x - d0 - k >= 0 ? (uint32_t)__popcll(a ^ r[-k]) : (uint32_t)invalid;
+        }
+        if (C1) {   // full scale of the multi-scale variant
+            const uint32_t h = *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + (x >> 1)) * D + (d0 >> 1));
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = (v[k] + ((h >> (8 * (k >> 1))) & 0xFFu) + 1) >> 1;
+        }
+        const uint32_t lo = v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24);
+        const uint32_t hi = v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24);
+        *(uint2 *)(row + (size_t)x * D + d0) = make_uint2(lo, hi);
+    }
+    __syncthreads();                                  // the tile memory may be reused next
+}
+
+}  // namespace tiles
+}  // namespace sgmgb
