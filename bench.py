@@ -338,6 +338,15 @@ def run_gb300(args):
     eng = sgmgb.Engine(local)
     eng.plan(W, H, D, PATHS)
     eng.set_path_shape(args.warps_per_block, args.disp_per_lane)
+    # frames in flight: each has its own context (resident workspace, stream,
+    # cached graph); consecutive frames alternate between them, so one frame's
+    # final pass overlaps the next frame's census, cost and first passes
+    engines = [eng]
+    for _ in range(args.inflight - 1):
+        e = sgmgb.Engine(local)
+        e.plan(W, H, D, PATHS)
+        e.set_path_shape(args.warps_per_block, args.disp_per_lane)
+        engines.append(e)
     # 8 distinct resident pairs, round-robin: inputs differ every step and the
     # per-frame working set (about 430 MB of census, scratch and sum planes)
     # is far larger than the 129 MB L2.
@@ -347,18 +356,35 @@ def run_gb300(args):
     dr = [torch.from_numpy(p[1]).to(dev) for p in pairs]
     dd = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(R)]
     s = torch.cuda.current_stream(dev)
+    streams = [s] + [torch.cuda.Stream(dev) for _ in range(args.inflight - 1)]
+    NF = len(engines)
+    assert R % NF == 0          # output buffer i % R is always written by the same context and stream
 
-    # correctness of what is timed: the first pair against the oracle (rank 0)
-    eng.run_frame_async(dl[0], dr[0], dd[0], stream=s)
-    s.synchronize()
+    # correctness of what is timed: the first pair through every context against the oracle (rank 0)
     bit_exact = None
     if rank == 0:
         import oracle
-        bit_exact = bool(np.array_equal(dd[0].cpu().numpy(), oracle.plain(pairs[0][0], pairs[0][1], D, PATHS)))
+        want = oracle.plain(pairs[0][0], pairs[0][1], D, PATHS)
+        bit_exact = True
+        for k, e in enumerate(engines):
+            e.run_frame_async(dl[0], dr[0], dd[0], stream=streams[k])
+            streams[k].synchronize()
+            bit_exact = bit_exact and bool(np.array_equal(dd[0].cpu().numpy(), want))
 
-    for i in range(args.warmup):
-        eng.run_frame_async(dl[i % R], dr[i % R], dd[i % R], stream=s)
-    s.synchronize()
+    def run_frames(n, nf):
+        for i in range(n):
+            engines[i % nf].run_frame_async(dl[i % R], dr[i % R], dd[i % R], stream=streams[i % nf])
+
+    run_frames(args.warmup, NF)
+    torch.cuda.synchronize(dev)
+    # one frame at a time (a single context and stream), for the frame latency
+    e0s, e1s = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n_serial = max(10, args.steps // 4)
+    e0s.record(s)
+    run_frames(n_serial, 1)
+    e1s.record(s)
+    torch.cuda.synchronize(dev)
+    serial_ms_per_frame = e0s.elapsed_time(e1s) / n_serial
 
     def barrier():
         if dist is not None:
@@ -372,8 +398,13 @@ def run_gb300(args):
     barrier()
     tw0 = time.time()
     ev0.record(s)
-    for i in range(args.steps):
-        eng.run_frame_async(dl[i % R], dr[i % R], dd[i % R], stream=s)
+    for st in streams[1:]:
+        st.wait_event(ev0)
+    run_frames(args.steps, NF)
+    for st in streams[1:]:
+        ev = torch.cuda.Event()
+        ev.record(st)
+        s.wait_event(ev)
     ev1.record(s)
     barrier()
     tw1 = time.time()
@@ -404,7 +435,8 @@ def run_gb300(args):
     kstats = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
 
     if rank != 0:
-        eng.close()
+        for e in engines:
+            e.close()
         if dist is not None:
             dist.destroy_process_group()
         return 0
@@ -418,8 +450,10 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u16", "data": "synthetic",
         "config": {"workload": WORKLOAD, "W": W, "H": H, "D": D, "paths": PATHS, "variant": "plain",
-                   "inputs": "8 resident synthetic pairs round-robin; per-frame working set ~430 MB > L2",
+                   "inputs": "8 resident synthetic pairs round-robin; per-frame working set 570 MB > L2",
+                   "frames_in_flight": NF,
                    "parallelism": "replicas" if ws > 1 else "single"},
+        "frame_latency_ms": serial_ms_per_frame,
         "fps": ws * args.steps / (ms / 1e3),
         "bit_exact_vs_oracle": bit_exact,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * W * H, "d2h_bytes_per_step": W * H,
@@ -442,7 +476,8 @@ def run_gb300(args):
         "clocks": clocks.summary(tw0, tw1),
         "gpu_launches": args.steps * KERNELS_PER_FRAME,
     }
-    eng.close()
+    for e in engines:
+        e.close()
     if not args.no_batch:
         line["batched"] = batched_section(sgmgb.Engine, sgmgb, torch, np)
     if not args.no_serve:
@@ -462,11 +497,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--warps-per-block", type=int, default=4, help="path-kernel shape (speed only)")
     ap.add_argument("--disp-per-lane", type=int, default=0, help="path-kernel shape: 0, 2, 4 or 8")
+    ap.add_argument("--inflight", type=int, default=4,
+                    help="frames in flight in the timed region (contexts and streams, round-robin)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form section")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-form section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.inflight not in (1, 2, 4, 8):
+        ap.error("--inflight must be 1, 2, 4 or 8")
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

@@ -43,8 +43,8 @@ __device__ __forceinline__ uint32_t window4(uint32_t w0, uint32_t w1, uint32_t w
 }
 
 // Census of the tile at (x0, y0) of one W x H image into out (W*H uint64).
-// nthreads: a multiple of 32; tid in [0, nthreads). ld_cg: read the image
-// through L2 only (it may have been written by another block of this launch).
+// nthreads: a multiple of 32; tid in [0, nthreads). The image is read through
+// the read-only path: it is an input, never written during the launch.
 __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint64_t *__restrict__ out,
                                             int W, int H, int x0, int y0, uint8_t *smem, int tid,
                                             int nthreads) {
@@ -113,9 +113,11 @@ __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint
 // conflicts), and each pixel's 32 bytes of the warp are one sector in the
 // store. The population counts (2 POPC per cost) are the bound.
 // ---------------------------------------------------------------------------
-constexpr int COST_PX = 64;
+constexpr int COST_PX = 64;                           // 8 blocks of 8 pixels, or 4 of 16
 constexpr int COST_SMEM = (COST_PX + COST_PX + 256) * 8;   // bytes, 16-byte aligned by the caller
 
+// LD_CG: read the descriptors through L2 only (the batch kernel, where other
+// blocks of the same launch wrote them); otherwise through the read-only path.
 template <bool LD_CG>
 __device__ __forceinline__ uint64_t ld_desc(const uint64_t *p) {
     return LD_CG ? __ldcg(p) : __ldg(p);
@@ -143,11 +145,12 @@ __device__ __forceinline__ void cost_tile(const uint64_t *__restrict__ cl, const
     const int DG = (tpp & 3) ? 2 : 4, PXW = 32 / DG;
     const int lane = tid & 31;
     const int pxl = DG == 4 ? lane >> 2 : lane >> 1, dgl = lane & (DG - 1);
-    const int nxb = COST_PX / PXW, ntask = nxb * (tpp / DG);
+    const int lnxb = DG == 4 ? 3 : 2;                 // log2(COST_PX / PXW)
+    const int ntask = (tpp / DG) << lnxb;
     const int hw = W >> 1;
     uint8_t *row = C + (size_t)y * W * D;
     for (int task = tid >> 5; task < ntask; task += nthreads >> 5) {
-        const int dgb = task / nxb, px = (task - dgb * nxb) * PXW + pxl;
+        const int dgb = task >> lnxb, px = (task & ((1 << lnxb) - 1)) * PXW + pxl;
         const int d0 = (dgb * DG + dgl) * 8, x = x0 + px;
         if (x >= W) continue;
         const uint64_t a = sl[px];
