@@ -198,8 +198,9 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
     uint32_t tot[NR];
 #pragma unroll
     for (int i = 0; i < NR; i++) {
-        tot[i] = __byte_perm(L[(2 * i) % NR] >> (16 * ((2 * i) / NR)),
-                             L[(2 * i + 1) % NR] >> (16 * ((2 * i + 1) / NR)), 0x5410);
+        if (NR == 1) tot[i] = L[0];   // register 0 is already (d0, d0+1)
+        else tot[i] = __byte_perm(L[(2 * i) % NR] >> (16 * ((2 * i) / NR)),
+                                  L[(2 * i + 1) % NR] >> (16 * ((2 * i + 1) / NR)), 0x5410);
         tot[i] += byte_pair(s.pw, i);
         if (MODE == MODE_FINAL3) tot[i] += byte_pair(s.pw + SCW, i) + byte_pair(s.pw + 2 * SCW, i);
         if (MODE == MODE_ACCUM || MODE == MODE_FINAL) tot[i] += s.sw[i];   // no carry: S <= 2040
@@ -220,7 +221,7 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
     if (KEY16) {
         uint32_t k = kFull;
 #pragma unroll
-        for (int i = 0; i < NR; i++) k = vmin2(k, (tot[i] << 6) + pk2((uint32_t)(d0 + 2 * i)) + 0x10000u);
+        for (int i = 0; i < NR; i++) k = vmin2(k, tot[i] * 64u + (pk2((uint32_t)(d0 + 2 * i)) + 0x10000u));
         key = live ? fold2(k) : kFull;
     } else {
         key = kFull;
@@ -396,10 +397,23 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
         const bool live = FULL ? active : i < len;
         uint32_t c[NR];
         unpack_cost<DPL, MODE>(s, c);
-        const uint32_t up = __shfl_up_sync(kFull, L[NR - 1], 1);
-        const uint32_t dn = __shfl_down_sync(kFull, L[0], 1);
-        const uint32_t lo0 = __byte_perm(up, L[NR - 1], 0x5432) | m_lo;   // (prev lane's last d, own d0+NR-1)
-        const uint32_t hiL = __byte_perm(L[0], dn, 0x5432) | m_hi;        // (own d0+NR, next lane's first d)
+        uint32_t lo0, hiL;
+        if (DPL == 2) {
+            // A lane's two disparities are neighbours. At a group's ends the
+            // width-limited shuffle returns the lane's own pair, so the missing
+            // d-1 (d+1) slot holds the d+1 (d-1) value: a duplicate of the other
+            // neighbour, which leaves min(lo, hi) unchanged -- no masks needed.
+            // (A pad lane past the last disparity holds L >= 255: also harmless.)
+            const uint32_t up = ONE ? __shfl_up_sync(kFull, L[0], 1) : __shfl_up_sync(kFull, L[0], 1, LPL);
+            const uint32_t dn = ONE ? __shfl_down_sync(kFull, L[0], 1) : __shfl_down_sync(kFull, L[0], 1, LPL);
+            lo0 = __byte_perm(up, L[0], 0x5432);     // (prev lane's d0+1, own d0)
+            hiL = __byte_perm(L[0], dn, 0x5432);     // (own d0+1, next lane's d0)
+        } else {
+            const uint32_t up = __shfl_up_sync(kFull, L[NR - 1], 1);
+            const uint32_t dn = __shfl_down_sync(kFull, L[0], 1);
+            lo0 = __byte_perm(up, L[NR - 1], 0x5432) | m_lo;   // (prev lane's last d, own d0+NR-1)
+            hiL = __byte_perm(L[0], dn, 0x5432) | m_hi;        // (own d0+NR, next lane's first d)
+        }
         uint32_t w[NR];
 #pragma unroll
         for (int j = 0; j < NR; j++) {
