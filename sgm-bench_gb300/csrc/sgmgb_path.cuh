@@ -174,15 +174,17 @@ __device__ __forceinline__ uint32_t byte_pair(const uint32_t *w, int i) {
 
 // What a pass does with L(p, d0..d0+DPL-1). `live`: this lane's line has a
 // pixel at this step; `lead`: the group's first lane; `gmask`: the group.
-// `out` points at this lane's bytes of pixel p in sc (SCRATCH) or S (STORE,
-// ACCUM). KEY16: the argmin key S*64 + d fits a packed u16 (4 paths, D <= 64).
+// `out` points at this lane's bytes of pixel p in S (STORE, ACCUM), or, for
+// SCRATCH, at its bytes of this step in the ring chunk's cost row, which the
+// chunk's end copies to the plane (there `live` only excludes pad lanes).
+// KEY16: the argmin key S*64 + d fits a packed u16 (4 paths, D <= 64).
 template <int DPL, int MODE, bool KEY16, bool ONE>
 __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int x, int y, int d0,
                                      bool lead, int g, uint32_t gmask, bool live, const uint32_t (&L)[DPL / 2],
                                      const StepIn<DPL, MODE> &s) {
     constexpr int NR = DPL / 2;
     constexpr int SCW = StepIn<DPL, MODE>::SCW;
-    if (MODE == MODE_SCRATCH) {
+    if (MODE == MODE_SCRATCH) {            // `out`: this lane's bytes in the ring's staging row
         if (!live) return;
         if (DPL == 2) {
             *(uint16_t *)out = (uint16_t)__byte_perm(L[0], 0, 0x0020);
@@ -306,6 +308,11 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
         goff[j] = ((long long)pg + (long long)k * step) * P.D + o;
         glim[j] = r < gD ? lg - k : 0;
     }
+    // SCRATCH: the plane has the cost volume's layout, so the chunk's L bytes,
+    // staged where its cost bytes were, go out by the same 16-byte granules.
+    long long ooff[NGB];
+#pragma unroll
+    for (int j = 0; j < NGB; j++) ooff[j] = goff[j];
     long long soff[HAS_S ? 2 * NGB : 1];
     int slim[HAS_S ? 2 * NGB : 1];
     if (HAS_S) {
@@ -356,7 +363,6 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
     // this lane's output for the current pixel: sc bytes (SCRATCH) or S words (STORE, ACCUM)
     uint8_t *out = nullptr;
     long long out_step = 0;
-    if (MODE == MODE_SCRATCH) { out = P.sc + (long long)p * P.D + d0; out_step = (long long)step * P.D; }
     if (MODE == MODE_STORE || MODE == MODE_ACCUM) {
         out = (uint8_t *)(P.S + (long long)p * P.D + d0); out_step = (long long)step * P.D * 2;
     }
@@ -384,17 +390,17 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
 #pragma unroll
     for (int j = 0; j < NR; j++) L[j] = has_d ? 0u : kPadPk;
     x -= dx; y -= dy; p -= step;
-    if (MODE != MODE_FINAL && MODE != MODE_FINAL3) out -= out_step;
+    if (MODE == MODE_STORE || MODE == MODE_ACCUM) out -= out_step;
 
     // One recurrence step on the next pixel of the line; FULL: every line of
     // the warp has this pixel (no per-step length test); ONE: the warp holds
     // one line (a plain full-warp reduction).
-    auto step_once = [&](const In &s, int i, auto full_t, auto one_t) {
+    auto step_once = [&](const In &s, int i, uint8_t *stage, auto full_t, auto one_t) {
         constexpr bool FULL = decltype(full_t)::value;
         constexpr bool ONE = decltype(one_t)::value;
         x += dx; y += dy; p += step;
-        if (MODE != MODE_FINAL && MODE != MODE_FINAL3) out += out_step;
-        const bool live = FULL ? active : i < len;
+        if (MODE == MODE_STORE || MODE == MODE_ACCUM) out += out_step;
+        const bool live = MODE == MODE_SCRATCH ? has_d : (FULL ? active : i < len);
         uint32_t c[NR];
         unpack_cost<DPL, MODE>(s, c);
         uint32_t lo0, hiL;
@@ -431,7 +437,8 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
             tm = vmin2(tm, v);
         }
         mn = ONE ? __reduce_min_sync(kFull, fold2(tm)) : group_min(fold2(tm), G, g, gmask);
-        emit<DPL, MODE, KEY16, ONE>(P, out, p, x, y, d0, lead, g, gmask, live, L, s);
+        emit<DPL, MODE, KEY16, ONE>(P, MODE == MODE_SCRATCH ? (void *)stage : (void *)out, p, x, y, d0, lead, g,
+                                    gmask, live, L, s);
     };
 
     // the chunk loop, instantiated for one line per warp and for several
@@ -440,16 +447,27 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
             cp_async_wait<NCH - 2>();   // chunk ch has landed (this lane's copies)
             __syncwarp();               // ... and every lane's; slot ch-1 is free
             issue(ch + NCH - 1);
-            const uint8_t *chunk = ring + (ch % NCH) * SLOT;
+            uint8_t *chunk = ring + (ch % NCH) * SLOT;
             In s[K];                    // the chunk's inputs, read before its steps run
 #pragma unroll
             for (int k = 0; k < K; k++) ring_read<DPL, MODE>(chunk, lane, k, s[k]);
             if ((ch + 1) * K <= minlen) {
 #pragma unroll
-                for (int k = 0; k < K; k++) step_once(s[k], ch * K + k, std::true_type{}, one_t);
+                for (int k = 0; k < K; k++)
+                    step_once(s[k], ch * K + k, chunk + k * SBM + lane * DPL, std::true_type{}, one_t);
             } else {
 #pragma unroll
-                for (int k = 0; k < K; k++) step_once(s[k], ch * K + k, std::false_type{}, one_t);
+                for (int k = 0; k < K; k++)
+                    step_once(s[k], ch * K + k, chunk + k * SBM + lane * DPL, std::false_type{}, one_t);
+            }
+            if (MODE == MODE_SCRATCH) {
+                __syncwarp();           // every lane's L bytes of the chunk are staged
+#pragma unroll
+                for (int j = 0; j < NGB; j++) {
+                    if (ch * K < glim[j])
+                        *(uint4 *)(P.sc + ooff[j]) = *(const uint4 *)(chunk + (lane + 32 * j) * 16);
+                    ooff[j] += adv;
+                }
             }
         }
     };
