@@ -1,0 +1,246 @@
+// sgmgb_pair.cuh -- the path recurrence with two lines per warp packed into
+// the halves of each register (the 4-path scratch and final passes, D = 32,
+// 64 or 128). Device code used by sgmgb_path.cu and sgmgb_batch.cu.
+//
+// Layout: a warp walks lines A and B of one direction together. Lane l owns
+// disparities d = l*NR .. l*NR + NR - 1 (NR = D/32), and register j of the
+// lane holds the packed pair (L_A[d], L_B[d]) for d = l*NR + j. Every
+// min.u16x2 and 32-bit add then advances both lines at once, the d-1 / d+1
+// neighbours of a register are its neighbouring registers (or one shuffle of
+// a whole register at the lane's ends) -- no byte permutes on the recurrence
+// -- and the minimum over d is a per-register minimum plus one warp reduction
+// per line: redux(tm & 0xffff) gives line A's minimum, and redux(tm) gives
+// line B's in its high half (the high half is the primary key of an unsigned
+// minimum).
+//
+// Ends of the disparity range: with NR <= 2 the width-32 shuffle returns the
+// lane's own register at lanes 0 and 31, so the missing d-1 (d+1) slot holds
+// the lane's own d+1 (d-1) value (NR = 2) or d itself (NR = 1): a duplicate
+// of the other neighbour or of prev[d], neither of which can lower
+// min(prev[d], lo + P1, hi + P1). With NR = 4 the slots are masked to 0x3FFF.
+//
+// Arithmetic as in sgmgb_path.cuh: no half carries (values < 0x8000), the
+// reference's saturations are no-ops (common/sgm_ref.c:61-72), and the first
+// pixel of a line starts from L_prev = 0, min_prev = 0, which yields L = C.
+//
+// Memory: the per-warp shared-memory ring of sgmgb_path.cuh, a step being the
+// two lines' D-byte rows [A | B] of each input stream; a chunk is 512 bytes of
+// a stream (one 16-byte cp.async granule per lane). The scratch output is
+// staged in the consumed cost rows and leaves by the same granules.
+#pragma once
+#include "sgmgb_path.cuh"
+
+namespace sgmgb {
+
+namespace {
+
+template <int NR> struct PairRing {
+    static constexpr int K = 8 / NR;                               // steps per chunk (512 B per stream)
+    static constexpr int NCH = NR == 1 ? 4 : (NR == 2 ? 6 : 10);   // ring depth in chunks
+    static constexpr int SB = 64 * NR;                             // bytes of one stream per step: [A | B]
+};
+template <int NR, int MODE> struct PairSlot {
+    static constexpr int U = MODE == MODE_FINAL3 ? 4 : 1;          // cost + the three planes
+    static constexpr int BYTES = 512 * U;
+    static constexpr int RING = PairRing<NR>::NCH * BYTES;
+};
+
+// NR bytes from shared memory, zero-extended into a word (NR = 1, 2) or a word (NR = 4).
+template <int NR>
+__device__ __forceinline__ uint32_t ld_run(const uint8_t *p) {
+    if (NR == 1) return *p;
+    if (NR == 2) return *(const uint16_t *)p;
+    return *(const uint32_t *)p;
+}
+
+// Registers of one stream for one step: out[j] = (A byte j, B byte j) as a u16 pair.
+template <int NR>
+__device__ __forceinline__ void pair_unpack(uint32_t a, uint32_t b, uint32_t (&out)[NR]) {
+    if (NR == 1) {
+        out[0] = __byte_perm(a, b, 0x5410);                        // a, b zero-extended bytes
+    } else if (NR == 2) {
+        out[0] = __byte_perm(a, b, 0x6420);
+        out[1] = __byte_perm(a, b, 0x6521);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++) out[j] = __byte_perm(a, b, j | ((4 + j) << 8)) & 0x00FF00FFu;
+    }
+}
+
+// The line-A bytes (low halves) or line-B bytes (high halves) of the registers, as NR packed bytes.
+template <int NR, bool HI>
+__device__ __forceinline__ uint32_t pair_pack(const uint32_t (&L)[NR]) {
+    constexpr uint32_t s = HI ? 0x62 : 0x40;                       // byte 0 (2) of x, byte 0 (2) of y
+    if (NR == 1) return HI ? (L[0] >> 16) & 0xFFu : L[0] & 0xFFu;
+    if (NR == 2) return __byte_perm(L[0], L[1], s);
+    return __byte_perm(__byte_perm(L[0], L[1], s), __byte_perm(L[2], L[3], s), 0x5410);
+}
+
+template <int NR>
+__device__ __forceinline__ void st_run(uint8_t *p, uint32_t v) {
+    if (NR == 1) *p = (uint8_t)v;
+    else if (NR == 2) *(uint16_t *)p = (uint16_t)v;
+    else *(uint32_t *)p = v;
+}
+
+// Entry pixel and length of `line` of direction (dx, dy).
+__device__ __forceinline__ void line_geo(const LineParams &P, int line, int &x, int &y, int &len) {
+    const int dx = P.dx, dy = P.dy;
+    const int xe = dx > 0 ? 0 : P.W - 1, ye = dy > 0 ? 0 : P.H - 1;
+    if (dy == 0) { x = xe; y = line; len = P.W; }
+    else if (dx == 0) { x = line; y = ye; len = P.H; }
+    else {
+        if (line < P.H) { x = xe; y = line; }
+        else { x = xe + dx * (line - P.H + 1); y = ye; }
+        len = min(dx > 0 ? P.W - x : x + 1, dy > 0 ? P.H - y : y + 1);
+    }
+    if (line >= P.nlines) len = 0;
+}
+
+}  // namespace
+
+// Runs warp `warp` of a scratch (MODE_SCRATCH: L into the plane P.sc) or
+// 4-path final pass (MODE_FINAL3: argmin of L + sc + sc2 + sc3 into P.disp)
+// over lines 2*warp and 2*warp+1. `ring`: this warp's PairSlot<NR, MODE>::RING
+// bytes of shared memory (16-byte aligned). All 32 lanes must call it.
+template <int NR, int MODE, bool KEY16>
+__device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t *ring) {
+    static_assert(MODE == MODE_SCRATCH || MODE == MODE_FINAL3, "pair layout: scratch and 4-path final passes");
+    constexpr int K = PairRing<NR>::K, NCH = PairRing<NR>::NCH, SB = PairRing<NR>::SB;
+    constexpr int U = PairSlot<NR, MODE>::U, SLOT = PairSlot<NR, MODE>::BYTES;
+    constexpr int D = 32 * NR;
+    const int lane = threadIdx.x & 31;
+    const int la = 2 * warp;
+    if (la >= P.nlines) return;                       // whole warp leaves together
+    int xa, ya, lena, xb, yb, lenb;
+    line_geo(P, la, xa, ya, lena);
+    line_geo(P, la + 1, xb, yb, lenb);                // lenb = 0 if there is no second line
+    const int maxlen = max(lena, lenb), minlen = lenb ? min(lena, lenb) : lena;
+    const int step = P.dy * P.W + P.dx;
+    int pa = ya * P.W + xa, pb = yb * P.W + xb;
+    const uint32_t P1 = pk2((uint32_t)P.p1), P2 = pk2((uint32_t)P.p2);
+    const uint32_t mlo = (NR == 4 && lane == 0) ? 0x3FFF3FFFu : 0u;    // d = -1 does not exist
+    const uint32_t mhi = (NR == 4 && lane == 31) ? 0x3FFF3FFFu : 0u;   // d = D does not exist
+
+    // this lane's 16-byte granule of every chunk: step k = b / SB, line b % SB / D, byte b % D
+    const uint32_t ring_s = (uint32_t)__cvta_generic_to_shared(ring);
+    const int gb = lane * 16, gk = gb / SB, gr = gb % SB, gl = gr / D, go = gr - gl * D;
+    const long long adv = (long long)K * step * D;
+    long long goff = ((long long)(gl ? pb : pa) + (long long)gk * step) * D + go;
+    const int glim = (gl ? lenb : lena) - gk;
+    long long ooff = goff;                            // scratch output: same granules, plane P.sc
+    const uint8_t *src[U];
+    src[0] = P.C;
+    if (MODE == MODE_FINAL3) { src[1] = P.sc; src[2] = P.sc2; src[3] = P.sc3; }
+    auto issue = [&](int c) {
+        const uint32_t dst = ring_s + (uint32_t)((c % NCH) * SLOT) + (uint32_t)gb;
+        if (c * K < glim) {
+#pragma unroll
+            for (int q = 0; q < U; q++) cp_async16(dst + (uint32_t)(q * 512), src[q] + goff);
+        }
+        goff += adv;
+        cp_async_commit();
+    };
+    const int nchunks = (maxlen + K - 1) / K;
+#pragma unroll
+    for (int c = 0; c < NCH - 1; c++) issue(c);
+
+    uint32_t L[NR];
+#pragma unroll
+    for (int j = 0; j < NR; j++) L[j] = 0u;
+    uint32_t mn = 0;                                  // L_prev = 0, min_prev = 0: the first step yields L = C
+    uint32_t dpk[NR];                                 // (d, d) for the argmin keys
+#pragma unroll
+    for (int j = 0; j < NR; j++) dpk[j] = pk2((uint32_t)(lane * NR + j));
+    pa -= step; pb -= step;
+
+    // one step of both lines; `in` = this step's rows in the chunk (stream q at q*512)
+    auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&pl)[3][NR], uint8_t *row, int i, auto full_t) {
+        constexpr bool FULL = decltype(full_t)::value;
+        pa += step; pb += step;
+        const uint32_t up = __shfl_up_sync(kFull, L[NR - 1], 1) | mlo;
+        const uint32_t dn = __shfl_down_sync(kFull, L[0], 1) | mhi;
+        uint32_t w[NR];
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const uint32_t lo = j == 0 ? up : L[j - 1];
+            const uint32_t hi = j == NR - 1 ? dn : L[j + 1];
+            w[j] = vmin2(L[j], vmin2(lo, hi) + P1);
+        }
+        const uint32_t E = mn + P2;
+        uint32_t tm = kFull;
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const uint32_t v = vmin2(w[j], E) + c[j] - mn;
+            L[j] = v;
+            tm = vmin2(tm, v);
+        }
+        const uint32_t ra = __reduce_min_sync(kFull, tm & 0xFFFFu);    // line A: low halves
+        const uint32_t rb = __reduce_min_sync(kFull, tm);              // line B: high half of the result
+        mn = __byte_perm(ra, rb, 0x7610);
+        if (MODE == MODE_SCRATCH) {
+            // stage both lines' L bytes in the consumed cost rows of this step
+            st_run<NR>(row + lane * NR, pair_pack<NR, false>(L));
+            st_run<NR>(row + D + lane * NR, pair_pack<NR, true>(L));
+        } else {
+            const bool live_a = FULL ? true : i < lena, live_b = FULL ? lenb > 0 : i < lenb;
+            uint32_t tot[NR];
+#pragma unroll
+            for (int j = 0; j < NR; j++) tot[j] = L[j] + pl[0][j] + pl[1][j] + pl[2][j];   // <= 4*254 per half
+            uint32_t da, db;
+            if (KEY16) {
+                uint32_t k = kFull;
+#pragma unroll
+                for (int j = 0; j < NR; j++) k = vmin2(k, tot[j] * 64u + dpk[j]);       // S*64 + d, lowest d on ties
+                da = __reduce_min_sync(kFull, k & 0xFFFFu) & 0x3Fu;
+                db = (__reduce_min_sync(kFull, k) >> 16) & 0x3Fu;
+            } else {
+                uint32_t ka = kFull, kb = kFull;
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    const uint32_t d = (uint32_t)(lane * NR + j);
+                    ka = min(ka, ((tot[j] & 0xFFFFu) << 8) | d);
+                    kb = min(kb, ((tot[j] >> 16) << 8) | d);
+                }
+                da = __reduce_min_sync(kFull, ka) & 0xFFu;
+                db = __reduce_min_sync(kFull, kb) & 0xFFu;
+            }
+            if (lane == 0) {
+                if (live_a) P.disp[pa] = (uint8_t)da;
+                if (live_b) P.disp[pb] = (uint8_t)db;
+            }
+        }
+    };
+
+    for (int ch = 0; ch < nchunks; ch++) {
+        cp_async_wait<NCH - 2>();                     // chunk ch has landed (this lane's copies)
+        __syncwarp();                                 // ... and every lane's; slot ch-1 is free
+        issue(ch + NCH - 1);
+        uint8_t *chunk = ring + (ch % NCH) * SLOT;
+        uint32_t c[K][NR], pl[K][3][NR];
+#pragma unroll
+        for (int k = 0; k < K; k++) {                 // the chunk's inputs, read before its steps run
+            const uint8_t *r = chunk + k * SB + lane * NR;
+            pair_unpack<NR>(ld_run<NR>(r), ld_run<NR>(r + D), c[k]);
+            if (MODE == MODE_FINAL3) {
+#pragma unroll
+                for (int q = 0; q < 3; q++) pair_unpack<NR>(ld_run<NR>(r + (q + 1) * 512), ld_run<NR>(r + (q + 1) * 512 + D), pl[k][q]);
+            }
+        }
+        if ((ch + 1) * K <= minlen) {
+#pragma unroll
+            for (int k = 0; k < K; k++) step_once(c[k], pl[k], chunk + k * SB, ch * K + k, std::true_type{});
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) step_once(c[k], pl[k], chunk + k * SB, ch * K + k, std::false_type{});
+        }
+        if (MODE == MODE_SCRATCH) {
+            __syncwarp();                             // every lane's L bytes of the chunk are staged
+            if (ch * K < glim) *(uint4 *)(P.sc + ooff) = *(const uint4 *)(chunk + gb);
+            ooff += adv;
+        }
+    }
+    cp_async_wait<0>();                               // no copy outlives the kernel
+}
+
+}  // namespace sgmgb
