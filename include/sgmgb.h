@@ -87,8 +87,11 @@ void sgmgb_destroy(sgmgb_ctx *ctx);
 /* Sizes the context's resident single-frame workspace (re-plans on change). */
 int  sgmgb_plan(sgmgb_ctx *ctx, const sgmgb_frame_desc *fd);
 /* Path-kernel shape of the context's frames: warps per block (1..4) and
- * disparities per lane (0, 2, 4 or 8, raised to the smallest value that fits
- * a line in one warp: 2 up to D = 64, 4 up to 128, 8 up to 256). Results do
+ * disparities per lane. 0 (the default) packs two lines per warp into the
+ * halves of each register for the scratch and 4-path final passes at D = 32,
+ * 64 and 128, and uses the smallest valid value elsewhere; 2, 4 or 8 (raised
+ * to the smallest value that fits a line in one warp: 2 up to D = 64, 4 up to
+ * 128, 8 up to 256) keeps one line per lane group for every pass. Results do
  * not depend on it, only speed. Drops cached graphs. */
 int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane);
 
@@ -172,9 +175,10 @@ int  sgmgb_batch_run(sgmgb_batch *b, const uint8_t *const *d_left,
  * wait for its inputs ran past the wait limit (the run was abandoned and the
  * outputs are undefined; the context stays usable). */
 int  sgmgb_batch_wait(sgmgb_batch *b);
-/* Times candidate shapes (warps per block 2 and 4; disparities per lane the
- * smallest valid and twice that) on these buffers, keeps the fastest, and,
- * when tune_cache is not NULL, records it for every frame description. */
+/* Times candidate shapes (warps per block 2 and 4; disparities per lane 0 --
+ * the two-lines-per-warp layout --, the smallest valid, and twice that) on
+ * these buffers, keeps the fastest, and, when tune_cache is not NULL, records
+ * it for every frame description. */
 int  sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left,
                           const uint8_t *const *d_right, uint8_t *const *d_disp,
                           const char *tune_cache);
@@ -191,8 +195,8 @@ void sgmgb_batch_destroy(sgmgb_batch *b);
 
 /* ---- autotuner cache (host-only; no GPU needed) ---- */
 /* Records / looks up the chosen path-kernel shape for a frame shape. The
- * cache file is a plain text table "W H D paths variant warps dpl us"; the
- * last matching line wins. */
+ * cache file is a plain text table "W H D paths variant warps dpl us" (dpl 0:
+ * two lines per warp); the last matching line wins. */
 int sgmgb_tune_lookup(const char *cache_path, const sgmgb_frame_desc *fd,
                       int *warps_per_block, int *disp_per_lane);
 int sgmgb_tune_record(const char *cache_path, const sgmgb_frame_desc *fd,

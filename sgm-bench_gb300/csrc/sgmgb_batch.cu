@@ -17,6 +17,7 @@
 #include "sgmgb_internal.h"
 #include "sgmgb_path.cuh"
 #include "sgmgb_tiles.cuh"
+#include "sgmgb_pair.cuh"
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -44,7 +45,7 @@ struct BPass {                   // one direction of one frame
     LineParams P;                // C, planes, S, W, H, D, nl/lpl/gpw, dx, dy, p1, p2, nlines, key16
     int frame;
     int mode;
-    int dpl;
+    int dpl;                     // disparities per lane; 0: two lines per warp (sgmgb_pair.cuh)
 };
 
 struct BItem {
@@ -113,6 +114,19 @@ __device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int wa
     LineParams P = bp.P;
     P.disp = disp;
     const bool key16 = P.key16 && P.D <= 64;
+    if (bp.dpl == 0) {                           // two lines per warp
+        const int nr = P.D >> 5;
+        if (bp.mode == MODE_SCRATCH) {
+            if (nr == 1) path_pair<1, MODE_SCRATCH, false>(P, warp, ring);
+            else if (nr == 2) path_pair<2, MODE_SCRATCH, false>(P, warp, ring);
+            else path_pair<4, MODE_SCRATCH, false>(P, warp, ring);
+        } else {
+            if (nr == 1) path_pair<1, MODE_FINAL3, true>(P, warp, ring);
+            else if (nr == 2) path_pair<2, MODE_FINAL3, true>(P, warp, ring);
+            else path_pair<4, MODE_FINAL3, false>(P, warp, ring);
+        }
+        return;
+    }
     switch (bp.dpl * 8 + bp.mode) {
     case 2 * 8 + MODE_SCRATCH: path_warp<2, MODE_SCRATCH, 0, false>(P, warp, ring); break;
     case 2 * 8 + MODE_STORE:   path_warp<2, MODE_STORE, 0, false>(P, warp, ring); break;
@@ -180,6 +194,20 @@ k_batch(const BItem *__restrict__ items, int n_items, const BFrame *__restrict__
 
 template <int DPL, int MODE> constexpr int ring_of() { return Slot<DPL, MODE>::RING; }
 
+// The pair layout serves the 4-path scratch and final passes at D = 32, 64, 128.
+bool pair_ok(int D, int paths, int mode) {
+    return paths == 4 && (mode == MODE_SCRATCH || mode == MODE_FINAL3) && (D == 32 || D == 64 || D == 128);
+}
+
+int pair_ring_bytes(int D, int mode) {
+    const bool f = mode == MODE_FINAL3;
+    switch (D) {
+    case 32: return f ? PairSlot<1, MODE_FINAL3>::RING : PairSlot<1, MODE_SCRATCH>::RING;
+    case 64: return f ? PairSlot<2, MODE_FINAL3>::RING : PairSlot<2, MODE_SCRATCH>::RING;
+    default: return f ? PairSlot<4, MODE_FINAL3>::RING : PairSlot<4, MODE_SCRATCH>::RING;
+    }
+}
+
 // Largest per-warp ring a pass of this shape needs.
 int ring_bytes_for(int dpl, int mode) {
     switch (dpl * 8 + mode) {
@@ -214,7 +242,7 @@ struct sgmgb_batch {
     sgmgb_ctx *ctx = nullptr;
     int n = 0;
     std::vector<sgmgb_frame_desc> fds;
-    std::vector<int> dpl;                 // per frame (resolved, >= smallest valid)
+    std::vector<int> dpl;                 // per frame: 0 (pair layout where it applies) or 2, 4, 8
     int wpb = 4;
     // device memory
     void *arena = nullptr;                // all frames' workspaces
@@ -276,7 +304,8 @@ int build_plan(sgmgb_batch *b) {
         base.C = s.C; base.sc = s.sc; base.S = s.S; base.disp = nullptr;
         base.W = fd.W; base.H = fd.H; base.D = fd.D; base.p1 = 20; base.p2 = 192;
         base.key16 = (fd.paths == 4 && fd.D <= 64) ? 1 : 0;
-        const int dpl = b->dpl[f];
+        const int fdpl = b->dpl[f];                  // 0: pair layout where it applies
+        const int dpl = fdpl ? fdpl : path_dpl(fd.D, 0);
         base.dpl = dpl;
         base.nl = fd.D / dpl; base.lpl = base.nl; base.gpw = (32 % base.lpl == 0) ? 32 / base.lpl : 1;
         struct Spec { int dx, dy, mode, phase; uint8_t *sc; const uint8_t *sc2, *sc3; };
@@ -300,11 +329,12 @@ int build_plan(sgmgb_batch *b) {
             bp.P.dx = sp.dx; bp.P.dy = sp.dy;
             bp.P.sc = sp.sc; bp.P.sc2 = sp.sc2; bp.P.sc3 = sp.sc3;
             bp.P.nlines = lines_for(fd.W, fd.H, sp.dx, sp.dy);
-            bp.frame = f; bp.mode = sp.mode; bp.dpl = dpl;
+            const bool pair = fdpl == 0 && pair_ok(fd.D, fd.paths, sp.mode);
+            bp.frame = f; bp.mode = sp.mode; bp.dpl = pair ? 0 : dpl;
             const int pi = (int)passes.size();
             passes.push_back(bp);
-            ring = std::max(ring, ring_bytes_for(dpl, sp.mode));
-            const int warps = (bp.P.nlines + bp.P.gpw - 1) / bp.P.gpw;
+            ring = std::max(ring, pair ? pair_ring_bytes(fd.D, sp.mode) : ring_bytes_for(dpl, sp.mode));
+            const int warps = pair ? (bp.P.nlines + 1) / 2 : (bp.P.nlines + bp.P.gpw - 1) / bp.P.gpw;
             const int nit = (warps + b->wpb - 1) / b->wpb;
             for (int j = 0; j < nit; j++) by_phase[sp.phase].push_back({IT_PATH, f, sp.phase, pi, j * b->wpb});
             b->need[(size_t)f * MAXPH + sp.phase] += nit;
@@ -399,7 +429,7 @@ int sgmgb_batch_create(sgmgb_ctx *ctx, const sgmgb_frame_desc *frames, int n, co
         const sgmgb_frame_desc &fd = frames[f];
         int w = 0, d = 0;
         const bool hit = tune_cache && sgmgb_tune_lookup(tune_cache, &fd, &w, &d) == SGMGB_OK;
-        b->dpl[f] = path_dpl(fd.D, hit ? d : 0);
+        b->dpl[f] = hit && d ? path_dpl(fd.D, d) : 0;
         const size_t sz = (size_t)fd.W * fd.H * fd.D;
         if (hit && sz > biggest) { biggest = sz; b->wpb = w; }
     }
@@ -484,11 +514,14 @@ int sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left, const uin
         return berr(b, SGMGB_ERR_CUDA, "autotune events");
     }
     float best = -1.f;
-    int best_w = saved_wpb, best_m = 1, rc = SGMGB_OK;
+    int best_w = saved_wpb, best_m = 0, rc = SGMGB_OK;
+    auto shape_of = [&](int f, int m) {   // m = 0: pair layout; 1, 2: smallest valid and twice that
+        return m ? path_dpl(b->fds[f].D, std::min(8, path_dpl(b->fds[f].D, 0) * m)) : 0;
+    };
     for (int w : {2, 4}) {
-        for (int m : {1, 2}) {
+        for (int m : {0, 1, 2}) {
             b->wpb = w;
-            for (int f = 0; f < b->n; f++) b->dpl[f] = path_dpl(b->fds[f].D, std::min(8, path_dpl(b->fds[f].D, 0) * m));
+            for (int f = 0; f < b->n; f++) b->dpl[f] = shape_of(f, m);
             if ((rc = build_plan(b))) goto done;
             if ((rc = sgmgb_batch_run(b, d_left, d_right, d_disp, nullptr)) || (rc = sgmgb_batch_wait(b))) goto done;
             float ms = 1e30f;
@@ -514,7 +547,7 @@ done:
         return rc;
     }
     b->wpb = best_w;
-    for (int f = 0; f < b->n; f++) b->dpl[f] = path_dpl(b->fds[f].D, std::min(8, path_dpl(b->fds[f].D, 0) * best_m));
+    for (int f = 0; f < b->n; f++) b->dpl[f] = shape_of(f, best_m);
     if ((rc = build_plan(b))) return rc;
     if (tune_cache) {
         for (int f = 0; f < b->n; f++) {

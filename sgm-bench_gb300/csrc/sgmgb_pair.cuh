@@ -36,7 +36,7 @@ namespace {
 
 template <int NR> struct PairRing {
     static constexpr int K = 8 / NR;                               // steps per chunk (512 B per stream)
-    static constexpr int NCH = NR == 1 ? 4 : (NR == 2 ? 6 : 10);   // ring depth in chunks
+    static constexpr int NCH = NR == 1 ? 4 : (NR == 2 ? 6 : 8);    // ring depth in chunks
     static constexpr int SB = 64 * NR;                             // bytes of one stream per step: [A | B]
 };
 template <int NR, int MODE> struct PairSlot {
