@@ -1,0 +1,117 @@
+"""sgmgb_cli: the reference-style command line (multiscale/sgm_ms_ref.c:151-217
+contract for `ms`; `plain` and `gen` beside it). PGM files in and out, the
+result line with the FNV hash, exit status 2 on a golden mismatch."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+import sgmgb
+
+CLI = os.path.join(os.path.dirname(sgmgb.LIB_PATH), "sgmgb_cli")
+
+
+def _have_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def write_pgm(path, a):
+    with open(path, "wb") as f:
+        f.write(b"P5\n# written by the test\n%d %d\n255\n" % (a.shape[1], a.shape[0]))
+        f.write(np.ascontiguousarray(a, np.uint8).tobytes())
+
+
+def read_pgm(path):
+    d = open(path, "rb").read()
+    i, tok = 2, []
+    while len(tok) < 3:
+        while d[i:i + 1].isspace():
+            i += 1
+        if d[i:i + 1] == b"#":
+            while d[i:i + 1] != b"\n":
+                i += 1
+            continue
+        j = i
+        while not d[j:j + 1].isspace():
+            j += 1
+        tok.append(int(d[i:j]))
+        i = j
+    w, h, _ = tok
+    return np.frombuffer(d[i + 1:i + 1 + w * h], np.uint8).reshape(h, w).copy()
+
+
+def run(*args):
+    return subprocess.run([CLI] + [str(a) for a in args], capture_output=True, text=True)
+
+
+def test_cli_usage_and_gen(tmp_path):
+    assert os.path.exists(CLI)
+    assert run().returncode == 1
+    assert run("ms").returncode == 1
+    p = run("gen", 96, 40, 64, 5, tmp_path)
+    assert p.returncode == 0, p.stderr
+    l, r, g = sgmgb.synth_pair(96, 40, 64, 5)
+    assert np.array_equal(read_pgm(str(tmp_path / "left.pgm")), l)
+    assert np.array_equal(read_pgm(str(tmp_path / "right.pgm")), r)
+    assert np.array_equal(read_pgm(str(tmp_path / "gt.pgm")), g)
+    assert run("gen", 0, 40, 64, 5, tmp_path).returncode == 1
+
+
+def test_cli_rejects_bad_input(tmp_path):
+    (tmp_path / "bad.pgm").write_bytes(b"P2\n2 2\n255\n0 0 0 0\n")
+    assert run("plain", tmp_path / "bad.pgm", tmp_path / "bad.pgm").returncode == 1
+    assert run("plain", tmp_path / "none.pgm", tmp_path / "none.pgm").returncode == 1
+
+
+@pytest.mark.skipif(_have_gpu(), reason="a GPU is present")
+def test_cli_without_gpu_fails_cleanly(tmp_path):
+    a = np.zeros((8, 8), np.uint8)
+    write_pgm(str(tmp_path / "a.pgm"), a)
+    p = run("plain", tmp_path / "a.pgm", tmp_path / "a.pgm")
+    assert p.returncode == 1 and "gb300" in p.stderr
+
+
+@pytest.mark.gpu
+def test_cli_multiscale_golden(tmp_path):
+    rng = np.random.default_rng(3)
+    l = rng.integers(0, 256, (66, 130), dtype=np.uint8)
+    r = rng.integers(0, 256, (66, 130), dtype=np.uint8)
+    write_pgm(str(tmp_path / "l.pgm"), l)
+    write_pgm(str(tmp_path / "r.pgm"), r)
+    want = oracle.multiscale(l, r)
+    write_pgm(str(tmp_path / "g.pgm"), want)
+    p = run("ms", tmp_path / "l.pgm", tmp_path / "r.pgm", "-g", tmp_path / "g.pgm", "-n", 3,
+            "-o", tmp_path / "o.pgm", "-j", tmp_path / "res.jsonl")
+    assert p.returncode == 0, p.stdout + p.stderr
+    line = p.stdout.strip()
+    assert line.startswith("ms_gb300  in 130x66 out 65x33 D=64 paths=8  median ") and line.endswith("GOLDEN OK")
+    assert ("hash " + oracle.fnv1a64(want)) in line
+    assert np.array_equal(read_pgm(str(tmp_path / "o.pgm")), want)
+    rec = json.loads(open(tmp_path / "res.jsonl").read().splitlines()[-1])
+    assert rec["impl"] == "ms_gb300" and rec["golden_match"] == 1 and rec["hash"] == oracle.fnv1a64(want)
+    bad = want.copy()
+    bad[0, 0] ^= 1
+    write_pgm(str(tmp_path / "bad.pgm"), bad)
+    p = run("ms", tmp_path / "l.pgm", tmp_path / "r.pgm", "-g", tmp_path / "bad.pgm")
+    assert p.returncode == 2 and p.stdout.strip().endswith("GOLDEN FAIL")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D,paths", [(64, 4), (128, 8)])
+def test_cli_plain_golden(tmp_path, D, paths):
+    l, r, _ = sgmgb.synth_pair(200, 90, D, 8)
+    write_pgm(str(tmp_path / "l.pgm"), l)
+    write_pgm(str(tmp_path / "r.pgm"), r)
+    want = oracle.plain(l, r, D, paths)
+    write_pgm(str(tmp_path / "g.pgm"), want)
+    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-D", D, "-p", paths, "-g", tmp_path / "g.pgm", "-n", 2)
+    assert p.returncode == 0, p.stdout + p.stderr
+    assert p.stdout.startswith("gb300  in 200x90 D=%d paths=%d" % (D, paths))
+    assert p.stdout.strip().endswith("GOLDEN OK")
