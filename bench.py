@@ -17,9 +17,11 @@ bytes of a frame (2*W*H*D + 3*W*H) to the pipelined frame time. `batched`
 runs the 96-pair mixed batch in one persistent launch against 96 sequential
 drop-in calls; `served` drives 8 virtual cameras with Poisson arrivals at
 2000 frames/s through the server and reports p50/p99 latency.
-`cpu_baseline` is the CPU oracle on a bounded sample of the same workload, one
-thread. `--impl reference` times the CPU oracle (the reference's algorithm,
-restated in C) on all host threads.
+`multiscale` times configurations B and C (the multi-scale 8-path variant at
+1920x800 and 1920x1080). `cpu_baseline` is the CPU oracle on a bounded sample of
+the same workload, one thread; that leg is also where the oracle checks the
+GPU's maps (`bit_exact_vs_oracle`). `--impl reference` times the CPU oracle
+(the reference's algorithm, restated in C) on all host threads.
 
 Multi-GPU: frames are independent, so N GPUs run N replicas (one process per
 GPU under torchrun); `value` is the frames of all ranks over the slowest
@@ -229,6 +231,9 @@ def served_section(eng_cls, sgmgb, np, rate=2000.0, secs=3.0):
             t_next += rng.exponential(1.0 / rate)
             if t_next > t_end:
                 break
+            gap = t_next - time.perf_counter()
+            if gap > 3e-4:
+                time.sleep(gap - 2e-4)      # sleeping releases the interpreter lock for the collector
             while time.perf_counter() < t_next:
                 pass
             c = int(rng.integers(0, 8))
@@ -250,11 +255,14 @@ def served_section(eng_cls, sgmgb, np, rate=2000.0, secs=3.0):
             o, _ = srv.wait(t, 60000)
             bad[0] += int(not np.array_equal(o, want[c][k]))
 
+    switch = sys.getswitchinterval()
+    sys.setswitchinterval(2e-4)             # the two client threads share the interpreter lock finely
     th = [threading.Thread(target=producer), threading.Thread(target=consumer)]
     for t in th:
         t.start()
     for t in th:
         t.join()
+    sys.setswitchinterval(switch)
     st = srv.stats()
     srv.close()
     eng.close()
@@ -266,21 +274,79 @@ def served_section(eng_cls, sgmgb, np, rate=2000.0, secs=3.0):
             "latency": "submit (host copy into pinned memory) to result in pinned host memory"}
 
 
-def cpu_baseline_sample(seconds=12.0):
-    """The oracle, one thread, on whole frames of the workload (at least one)."""
+def cpu_baseline_sample(seconds, left, right, gpu_maps, ms_checks=()):
+    """The CPU leg: the oracle (the reference's scalar algorithm restated in C),
+    one thread, timed on whole frames of the workload -- the very pair the GPU
+    timed first -- and used as the checker of the GPU's maps: `gpu_maps` are the
+    maps every timed context made of that pair, `ms_checks` (left, right, map)
+    multi-scale maps of the multiscale section."""
+    import numpy as np
     import oracle
-    import sgmgb
-    left, right, _ = sgmgb.synth_pair(W, H, D, 101)
     n, t0 = 0, time.perf_counter()
     while True:
-        oracle.plain(left, right, D, PATHS)
+        want = oracle.plain(left, right, D, PATHS)
         n += 1
         el = time.perf_counter() - t0
         if el >= seconds or n >= 8:
             break
+    exact = all(np.array_equal(m, want) for m in gpu_maps)
+    ms_exact = all(np.array_equal(m, oracle.multiscale(l, r)) for l, r, m in ms_checks) if ms_checks else None
     return {"value": n * W * H * D / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": "%d frame(s) of %dx%d D=%d %d-path, oracle/sgm_oracle.c, 1 thread, %.1f s"
-                      % (n, W, H, D, PATHS, el)}
+                      % (n, W, H, D, PATHS, el)}, exact, ms_exact
+
+
+def multiscale_section(sgmgb, torch, np, steps=60, inflight=4):
+    """Configurations B and C: the multi-scale 8-path variant at 1920x800 and
+    1920x1080 (output (W/2)x(H/2)), frames in flight as in the main line;
+    MDE/s under the reference's work convention ((W/2)(H/2) + W*H) * 64 per
+    second (multiscale/sgm_ms_ref.c:211-216). Returns the section and, per
+    configuration, one (left, right, map) for the CPU leg's oracle check."""
+    out, checks = {}, []
+    for name, (Wm, Hm) in (("configB_1920x800", (1920, 800)), ("configC_1920x1080", (1920, 1080))):
+        engs = []
+        for _ in range(inflight):
+            e = sgmgb.Engine(0)
+            e.plan(Wm, Hm, 64, 8, sgmgb.MULTISCALE)
+            engs.append(e)
+        strs = [torch.cuda.current_stream()] + [torch.cuda.Stream() for _ in range(inflight - 1)]
+        pairs = [sgmgb.synth_pair(Wm, Hm, 64, 300 + k) for k in range(inflight)]
+        dl = [torch.from_numpy(p[0]).cuda() for p in pairs]
+        dr = [torch.from_numpy(p[1]).cuda() for p in pairs]
+        dd = [torch.empty((Hm // 2, Wm // 2), dtype=torch.uint8, device="cuda") for _ in range(inflight)]
+        for i in range(2 * inflight):                                 # warm-up (graphs captured)
+            engs[i % inflight].run_frame_async(dl[i % inflight], dr[i % inflight], dd[i % inflight],
+                                               stream=strs[i % inflight])
+        torch.cuda.synchronize()
+        checks.append((pairs[0][0], pairs[0][1], dd[0].cpu().numpy()))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0 = strs[0]
+        e0.record(s0)
+        for st in strs[1:]:
+            st.wait_event(e0)
+        for i in range(steps):
+            engs[i % inflight].run_frame_async(dl[i % inflight], dr[i % inflight], dd[i % inflight],
+                                               stream=strs[i % inflight])
+        for st in strs[1:]:
+            ev = torch.cuda.Event()
+            ev.record(st)
+            s0.wait_event(ev)
+        e1.record(s0)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        # one frame at a time, host buffers (the drop-in call)
+        engs[0].run_frame(pairs[0][0], pairs[0][1])
+        t0 = time.perf_counter()
+        for _ in range(10):
+            engs[0].run_frame(pairs[0][0], pairs[0][1])
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / 10
+        work = ((Wm // 2) * (Hm // 2) + Wm * Hm) * 64
+        out[name] = {"W": Wm, "H": Hm, "out": [Wm // 2, Hm // 2], "ms_per_frame": ms, "fps": 1e3 / ms,
+                     "mde_per_s_work": work / (ms / 1e3) / 1e6, "frames_in_flight": inflight,
+                     "e2e_ms_per_frame": e2e_ms, "e2e_fps": 1e3 / e2e_ms}
+        for e in engs:
+            e.close()
+    return out, checks
 
 
 def run_reference(args):
@@ -360,16 +426,12 @@ def run_gb300(args):
     NF = len(engines)
     assert R % NF == 0          # output buffer i % R is always written by the same context and stream
 
-    # correctness of what is timed: the first pair through every context against the oracle (rank 0)
-    bit_exact = None
-    if rank == 0:
-        import oracle
-        want = oracle.plain(pairs[0][0], pairs[0][1], D, PATHS)
-        bit_exact = True
-        for k, e in enumerate(engines):
-            e.run_frame_async(dl[0], dr[0], dd[0], stream=streams[k])
-            streams[k].synchronize()
-            bit_exact = bit_exact and bool(np.array_equal(dd[0].cpu().numpy(), want))
+    # what is timed, for the checker in the CPU leg: the first pair through every context
+    maps0 = []
+    for k, e in enumerate(engines):
+        e.run_frame_async(dl[0], dr[0], dd[0], stream=streams[k])
+        streams[k].synchronize()
+        maps0.append(dd[0].cpu().numpy())
 
     def run_frames(n, nf):
         for i in range(n):
@@ -455,7 +517,7 @@ def run_gb300(args):
                    "parallelism": "replicas" if ws > 1 else "single"},
         "frame_latency_ms": serial_ms_per_frame,
         "fps": ws * args.steps / (ms / 1e3),
-        "bit_exact_vs_oracle": bit_exact,
+        "bit_exact_vs_oracle": None,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * W * H, "d2h_bytes_per_step": W * H,
                 "fps": ws * e2e_steps / e2e_s, "p50_ms": statistics.median(lat) * 1e3,
                 "p99_ms": sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
@@ -472,12 +534,19 @@ def run_gb300(args):
         "kernels": [{"name": k[0], "ms": round(k[1], 5), "algorithmic_bytes": k[2],
                      "gbs": round(k[2] / (k[1] / 1e3) / 1e9, 1)} for k in kstats],
         "frame_ms_kernels_alone": frame_ms_alone,
-        "cpu_baseline": cpu_baseline_sample(args.cpu_seconds),
+        "cpu_baseline": None,
         "clocks": clocks.summary(tw0, tw1),
         "gpu_launches": args.steps * KERNELS_PER_FRAME,
     }
     for e in engines:
         e.close()
+    ms_checks = ()
+    if not args.no_multiscale:
+        line["multiscale"], ms_checks = multiscale_section(sgmgb, torch, np)
+    line["cpu_baseline"], line["bit_exact_vs_oracle"], ms_exact = cpu_baseline_sample(
+        args.cpu_seconds, pairs[0][0], pairs[0][1], maps0, ms_checks)
+    if ms_exact is not None:
+        line["multiscale"]["bit_exact_vs_oracle"] = ms_exact
     if not args.no_batch:
         line["batched"] = batched_section(sgmgb.Engine, sgmgb, torch, np)
     if not args.no_serve:
@@ -500,6 +569,7 @@ def main():
     ap.add_argument("--inflight", type=int, default=4,
                     help="frames in flight in the timed region (contexts and streams, round-robin)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form section")
+    ap.add_argument("--no-multiscale", action="store_true", help="skip the configurations B/C section")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-form section")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -35,7 +35,7 @@ using Clock = std::chrono::steady_clock;
 
 namespace {
 
-constexpr int kReqBufsPerCamera = 8;
+constexpr int kReqBufsPerCamera = 16;
 constexpr int kMaxSlotsPerCamera = 4;
 
 struct Camera;

@@ -94,7 +94,7 @@ def test_server_refuses_when_request_buffers_run_out(engine):
     s = sgmgb.Server(engine, max_inflight=1)
     s.add_camera(5, 64, 48, 64, 4)
     l, r, _ = sgmgb.synth_pair(64, 48, 64, seed=9)
-    tickets = [s.submit(5, l, r) for _ in range(8)]    # 8 request buffers per camera
+    tickets = [s.submit(5, l, r) for _ in range(16)]   # 16 request buffers per camera
     with pytest.raises(sgmgb.SgmError) as ei:
         s.submit(5, l, r)
     assert ei.value.code == sgmgb.ERR_BUDGET
