@@ -115,15 +115,22 @@ __device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int wa
     P.disp = disp;
     const bool key16 = P.key16 && P.D <= 64;
     if (bp.dpl == 0) {                           // two lines per warp
-        const int nr = P.D >> 5;
-        if (bp.mode == MODE_SCRATCH) {
-            if (nr == 1) path_pair<1, MODE_SCRATCH, false>(P, warp, ring);
-            else if (nr == 2) path_pair<2, MODE_SCRATCH, false>(P, warp, ring);
-            else path_pair<4, MODE_SCRATCH, false>(P, warp, ring);
-        } else {
-            if (nr == 1) path_pair<1, MODE_FINAL3, true>(P, warp, ring);
-            else if (nr == 2) path_pair<2, MODE_FINAL3, true>(P, warp, ring);
-            else path_pair<4, MODE_FINAL3, false>(P, warp, ring);
+        switch ((P.D >> 5) * 8 + bp.mode) {
+        case 1 * 8 + MODE_SCRATCH: path_pair<1, MODE_SCRATCH, 0, false>(P, warp, ring); break;
+        case 1 * 8 + MODE_STORE:   path_pair<1, MODE_STORE, 0, false>(P, warp, ring); break;
+        case 1 * 8 + MODE_ACCUM:   path_pair<1, MODE_ACCUM, 0, false>(P, warp, ring); break;
+        case 1 * 8 + MODE_FINAL:   path_pair<1, MODE_FINAL, 0, false>(P, warp, ring); break;
+        case 1 * 8 + MODE_FINAL3:  path_pair<1, MODE_FINAL3, 0, true>(P, warp, ring); break;
+        case 2 * 8 + MODE_SCRATCH: path_pair<2, MODE_SCRATCH, 0, false>(P, warp, ring); break;
+        case 2 * 8 + MODE_STORE:   path_pair<2, MODE_STORE, 0, false>(P, warp, ring); break;
+        case 2 * 8 + MODE_ACCUM:   path_pair<2, MODE_ACCUM, 0, false>(P, warp, ring); break;
+        case 2 * 8 + MODE_FINAL:   path_pair<2, MODE_FINAL, 0, false>(P, warp, ring); break;
+        case 2 * 8 + MODE_FINAL3:  path_pair<2, MODE_FINAL3, 0, true>(P, warp, ring); break;
+        case 4 * 8 + MODE_SCRATCH: path_pair<4, MODE_SCRATCH, 0, false>(P, warp, ring); break;
+        case 4 * 8 + MODE_STORE:   path_pair<4, MODE_STORE, 0, false>(P, warp, ring); break;
+        case 4 * 8 + MODE_ACCUM:   path_pair<4, MODE_ACCUM, 0, false>(P, warp, ring); break;
+        case 4 * 8 + MODE_FINAL:   path_pair<4, MODE_FINAL, 0, false>(P, warp, ring); break;
+        default:                   path_pair<4, MODE_FINAL3, 0, false>(P, warp, ring); break;
         }
         return;
     }
@@ -194,18 +201,22 @@ k_batch(const BItem *__restrict__ items, int n_items, const BFrame *__restrict__
 
 template <int DPL, int MODE> constexpr int ring_of() { return Slot<DPL, MODE>::RING; }
 
-// The pair layout serves the 4-path scratch and final passes at D = 32, 64, 128.
-bool pair_ok(int D, int paths, int mode) {
-    return paths == 4 && (mode == MODE_SCRATCH || mode == MODE_FINAL3) && (D == 32 || D == 64 || D == 128);
+// The pair layout serves every pass at D = 32, 64, 128.
+bool pair_ok(int D) { return D == 32 || D == 64 || D == 128; }
+
+template <int NR>
+int pair_ring_nr(int mode) {
+    switch (mode) {
+    case MODE_SCRATCH: return PairSlot<NR, MODE_SCRATCH>::RING;
+    case MODE_STORE:   return PairSlot<NR, MODE_STORE>::RING;
+    case MODE_ACCUM:   return PairSlot<NR, MODE_ACCUM>::RING;
+    case MODE_FINAL:   return PairSlot<NR, MODE_FINAL>::RING;
+    default:           return PairSlot<NR, MODE_FINAL3>::RING;
+    }
 }
 
 int pair_ring_bytes(int D, int mode) {
-    const bool f = mode == MODE_FINAL3;
-    switch (D) {
-    case 32: return f ? PairSlot<1, MODE_FINAL3>::RING : PairSlot<1, MODE_SCRATCH>::RING;
-    case 64: return f ? PairSlot<2, MODE_FINAL3>::RING : PairSlot<2, MODE_SCRATCH>::RING;
-    default: return f ? PairSlot<4, MODE_FINAL3>::RING : PairSlot<4, MODE_SCRATCH>::RING;
-    }
+    return D == 32 ? pair_ring_nr<1>(mode) : (D == 64 ? pair_ring_nr<2>(mode) : pair_ring_nr<4>(mode));
 }
 
 // Largest per-warp ring a pass of this shape needs.
@@ -329,7 +340,7 @@ int build_plan(sgmgb_batch *b) {
             bp.P.dx = sp.dx; bp.P.dy = sp.dy;
             bp.P.sc = sp.sc; bp.P.sc2 = sp.sc2; bp.P.sc3 = sp.sc3;
             bp.P.nlines = lines_for(fd.W, fd.H, sp.dx, sp.dy);
-            const bool pair = fdpl == 0 && pair_ok(fd.D, fd.paths, sp.mode);
+            const bool pair = fdpl == 0 && pair_ok(fd.D);
             bp.frame = f; bp.mode = sp.mode; bp.dpl = pair ? 0 : dpl;
             const int pi = (int)passes.size();
             passes.push_back(bp);

@@ -1,6 +1,6 @@
 // sgmgb_pair.cuh -- the path recurrence with two lines per warp packed into
-// the halves of each register (the 4-path scratch and final passes, D = 32,
-// 64 or 128). Device code used by sgmgb_path.cu and sgmgb_batch.cu.
+// the halves of each register (every pass mode, D = 32, 64 or 128). Device
+// code used by sgmgb_path.cu and sgmgb_batch.cu.
 //
 // Layout: a warp walks lines A and B of one direction together. Lane l owns
 // disparities d = l*NR .. l*NR + NR - 1 (NR = D/32), and register j of the
@@ -39,8 +39,13 @@ template <int NR> struct PairRing {
     static constexpr int NCH = NR == 1 ? 4 : (NR == 2 ? 6 : 8);    // ring depth in chunks
     static constexpr int SB = 64 * NR;                             // bytes of one stream per step: [A | B]
 };
+// Streams of a chunk slot, in 512-byte units: the cost bytes, the planes the
+// pass reads (one: sc; three for FINAL3), and the partial sum S (uint16, two
+// units) for ACCUM and FINAL.
 template <int NR, int MODE> struct PairSlot {
-    static constexpr int U = MODE == MODE_FINAL3 ? 4 : 1;          // cost + the three planes
+    static constexpr int NPL = MODE == MODE_SCRATCH ? 0 : (MODE == MODE_FINAL3 ? 3 : 1);
+    static constexpr bool HAS_S = MODE == MODE_ACCUM || MODE == MODE_FINAL;
+    static constexpr int U = 1 + NPL + (HAS_S ? 2 : 0);
     static constexpr int BYTES = 512 * U;
     static constexpr int RING = PairRing<NR>::NCH * BYTES;
 };
@@ -76,6 +81,31 @@ __device__ __forceinline__ uint32_t pair_pack(const uint32_t (&L)[NR]) {
     return __byte_perm(__byte_perm(L[0], L[1], s), __byte_perm(L[2], L[3], s), 0x5410);
 }
 
+// NR uint16 sums of line A (sa) and of line B (sb), as words, into packed (A[d], B[d]) registers.
+template <int NR>
+__device__ __forceinline__ void pair_unpack16(const uint32_t *sa, const uint32_t *sb, uint32_t (&out)[NR]) {
+    if (NR == 1) {
+        out[0] = __byte_perm(sa[0], sb[0], 0x5410);
+    } else {
+#pragma unroll
+        for (int w = 0; w < NR / 2; w++) {
+            out[2 * w] = __byte_perm(sa[w], sb[w], 0x5410);
+            out[2 * w + 1] = __byte_perm(sa[w], sb[w], 0x7632);
+        }
+    }
+}
+
+// The line-A (HI = false) or line-B halves of NR packed registers as NR uint16 values, in words.
+template <int NR, bool HI>
+__device__ __forceinline__ void pair_pack16(const uint32_t (&t)[NR], uint32_t *w) {
+    constexpr uint32_t s = HI ? 0x7632 : 0x5410;
+    if (NR == 1) w[0] = HI ? t[0] >> 16 : t[0] & 0xFFFFu;
+    else {
+#pragma unroll
+        for (int i = 0; i < NR / 2; i++) w[i] = __byte_perm(t[2 * i], t[2 * i + 1], s);
+    }
+}
+
 template <int NR>
 __device__ __forceinline__ void st_run(uint8_t *p, uint32_t v) {
     if (NR == 1) *p = (uint8_t)v;
@@ -99,16 +129,21 @@ __device__ __forceinline__ void line_geo(const LineParams &P, int line, int &x, 
 
 }  // namespace
 
-// Runs warp `warp` of a scratch (MODE_SCRATCH: L into the plane P.sc) or
-// 4-path final pass (MODE_FINAL3: argmin of L + sc + sc2 + sc3 into P.disp)
-// over lines 2*warp and 2*warp+1. `ring`: this warp's PairSlot<NR, MODE>::RING
+// Runs warp `warp` of a pass over lines 2*warp and 2*warp+1, in any mode:
+//   SCRATCH  L into the plane P.sc
+//   STORE    S = sc + L            ACCUM  S += sc + L
+//   FINAL    argmin(S + sc + L)    FINAL3 argmin(L + sc + sc2 + sc3) into P.disp
+// (the even-only map of the multi-scale variant in FINAL). SAT: clamp L to
+// 255 (multiscale/sgm_ms_ref.c:82). `ring`: this warp's PairSlot<NR, MODE>::RING
 // bytes of shared memory (16-byte aligned). All 32 lanes must call it.
-template <int NR, int MODE, bool KEY16>
+template <int NR, int MODE, int SAT, bool KEY16>
 __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t *ring) {
-    static_assert(MODE == MODE_SCRATCH || MODE == MODE_FINAL3, "pair layout: scratch and 4-path final passes");
     constexpr int K = PairRing<NR>::K, NCH = PairRing<NR>::NCH, SB = PairRing<NR>::SB;
-    constexpr int U = PairSlot<NR, MODE>::U, SLOT = PairSlot<NR, MODE>::BYTES;
+    constexpr int NPL = PairSlot<NR, MODE>::NPL;
+    constexpr bool HAS_S = PairSlot<NR, MODE>::HAS_S;
+    constexpr int SLOT = PairSlot<NR, MODE>::BYTES;
     constexpr int D = 32 * NR;
+    constexpr bool FIN = MODE == MODE_FINAL || MODE == MODE_FINAL3;
     const int lane = threadIdx.x & 31;
     const int la = 2 * warp;
     if (la >= P.nlines) return;                       // whole warp leaves together
@@ -116,29 +151,48 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     line_geo(P, la, xa, ya, lena);
     line_geo(P, la + 1, xb, yb, lenb);                // lenb = 0 if there is no second line
     const int maxlen = max(lena, lenb), minlen = lenb ? min(lena, lenb) : lena;
-    const int step = P.dy * P.W + P.dx;
+    const int dx = P.dx, dy = P.dy, step = dy * P.W + dx;
     int pa = ya * P.W + xa, pb = yb * P.W + xb;
     const uint32_t P1 = pk2((uint32_t)P.p1), P2 = pk2((uint32_t)P.p2);
     const uint32_t mlo = (NR == 4 && lane == 0) ? 0x3FFF3FFFu : 0u;    // d = -1 does not exist
     const uint32_t mhi = (NR == 4 && lane == 31) ? 0x3FFF3FFFu : 0u;   // d = D does not exist
 
-    // this lane's 16-byte granule of every chunk: step k = b / SB, line b % SB / D, byte b % D
+    // this lane's 16-byte granules of every chunk. Byte streams (cost, planes):
+    // step k = b / SB, line b % SB / D, byte b % D. The sum S (2 units): two
+    // granules, step b / (2 SB), line b % (2 SB) / (2D), byte b % (2D).
     const uint32_t ring_s = (uint32_t)__cvta_generic_to_shared(ring);
     const int gb = lane * 16, gk = gb / SB, gr = gb % SB, gl = gr / D, go = gr - gl * D;
     const long long adv = (long long)K * step * D;
     long long goff = ((long long)(gl ? pb : pa) + (long long)gk * step) * D + go;
     const int glim = (gl ? lenb : lena) - gk;
     long long ooff = goff;                            // scratch output: same granules, plane P.sc
-    const uint8_t *src[U];
+    long long soff[2];
+    int slim[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int b = (lane + 32 * h) * 16, k = b / (2 * SB), r = b % (2 * SB), l = r / (2 * D), o = r - l * 2 * D;
+        soff[h] = ((long long)(l ? pb : pa) + (long long)k * step) * 2 * D + o;
+        slim[h] = HAS_S ? (l ? lenb : lena) - k : 0;
+    }
+    const uint8_t *src[1 + NPL];
     src[0] = P.C;
-    if (MODE == MODE_FINAL3) { src[1] = P.sc; src[2] = P.sc2; src[3] = P.sc3; }
+    if (NPL >= 1) src[1] = P.sc;
+    if (NPL == 3) { src[2] = P.sc2; src[3] = P.sc3; }
     auto issue = [&](int c) {
-        const uint32_t dst = ring_s + (uint32_t)((c % NCH) * SLOT) + (uint32_t)gb;
+        const uint32_t dst = ring_s + (uint32_t)((c % NCH) * SLOT);
         if (c * K < glim) {
 #pragma unroll
-            for (int q = 0; q < U; q++) cp_async16(dst + (uint32_t)(q * 512), src[q] + goff);
+            for (int q = 0; q <= NPL; q++) cp_async16(dst + (uint32_t)(q * 512 + gb), src[q] + goff);
         }
         goff += adv;
+        if (HAS_S) {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (c * K < slim[h])
+                    cp_async16(dst + (uint32_t)((1 + NPL) * 512 + (lane + 32 * h) * 16), (const uint8_t *)P.S + soff[h]);
+                soff[h] += 2 * adv;
+            }
+        }
         cp_async_commit();
     };
     const int nchunks = (maxlen + K - 1) / K;
@@ -152,12 +206,14 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     uint32_t dpk[NR];                                 // (d, d) for the argmin keys
 #pragma unroll
     for (int j = 0; j < NR; j++) dpk[j] = pk2((uint32_t)(lane * NR + j));
-    pa -= step; pb -= step;
+    pa -= step; pb -= step; xa -= dx; ya -= dy; xb -= dx; yb -= dy;
+    const int hw = P.W >> 1;
 
-    // one step of both lines; `in` = this step's rows in the chunk (stream q at q*512)
-    auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&pl)[3][NR], uint8_t *row, int i, auto full_t) {
+    // one step of both lines; `row`: this step's cost row in the chunk
+    auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&pl)[3][NR], const uint32_t (&sv)[NR], uint8_t *row,
+                         int i, auto full_t) {
         constexpr bool FULL = decltype(full_t)::value;
-        pa += step; pb += step;
+        pa += step; pb += step; xa += dx; ya += dy; xb += dx; yb += dy;
         const uint32_t up = __shfl_up_sync(kFull, L[NR - 1], 1) | mlo;
         const uint32_t dn = __shfl_down_sync(kFull, L[0], 1) | mhi;
         uint32_t w[NR];
@@ -171,41 +227,69 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         uint32_t tm = kFull;
 #pragma unroll
         for (int j = 0; j < NR; j++) {
-            const uint32_t v = vmin2(w[j], E) + c[j] - mn;
+            uint32_t v = vmin2(w[j], E) + c[j] - mn;
+            if (SAT) v = vmin2(v, 0x00FF00FFu);
             L[j] = v;
             tm = vmin2(tm, v);
         }
         const uint32_t ra = __reduce_min_sync(kFull, tm & 0xFFFFu);    // line A: low halves
         const uint32_t rb = __reduce_min_sync(kFull, tm);              // line B: high half of the result
         mn = __byte_perm(ra, rb, 0x7610);
+        const bool live_a = FULL ? true : i < lena, live_b = FULL ? lenb > 0 : i < lenb;
         if (MODE == MODE_SCRATCH) {
-            // stage both lines' L bytes in the consumed cost rows of this step
+            // stage both lines' L bytes in the consumed cost row of this step
             st_run<NR>(row + lane * NR, pair_pack<NR, false>(L));
             st_run<NR>(row + D + lane * NR, pair_pack<NR, true>(L));
-        } else {
-            const bool live_a = FULL ? true : i < lena, live_b = FULL ? lenb > 0 : i < lenb;
-            uint32_t tot[NR];
+            return;
+        }
+        uint32_t tot[NR];                             // this pass's L plus what the pass reads, per half <= 8*255
 #pragma unroll
-            for (int j = 0; j < NR; j++) tot[j] = L[j] + pl[0][j] + pl[1][j] + pl[2][j];   // <= 4*254 per half
-            uint32_t da, db;
-            if (KEY16) {
-                uint32_t k = kFull;
-#pragma unroll
-                for (int j = 0; j < NR; j++) k = vmin2(k, tot[j] * 64u + dpk[j]);       // S*64 + d, lowest d on ties
-                da = __reduce_min_sync(kFull, k & 0xFFFFu) & 0x3Fu;
-                db = (__reduce_min_sync(kFull, k) >> 16) & 0x3Fu;
+        for (int j = 0; j < NR; j++) {
+            tot[j] = L[j] + pl[0][j];
+            if (MODE == MODE_FINAL3) tot[j] += pl[1][j] + pl[2][j];
+            if (HAS_S) tot[j] += sv[j];
+        }
+        if (MODE == MODE_STORE || MODE == MODE_ACCUM) {
+            uint32_t wa[NR > 1 ? NR / 2 : 1], wb[NR > 1 ? NR / 2 : 1];
+            pair_pack16<NR, false>(tot, wa);
+            pair_pack16<NR, true>(tot, wb);
+            uint16_t *Sa = P.S + (long long)pa * D + lane * NR, *Sb = P.S + (long long)pb * D + lane * NR;
+            if (NR == 1) {
+                if (live_a) *Sa = (uint16_t)wa[0];
+                if (live_b) *Sb = (uint16_t)wb[0];
+            } else if (NR == 2) {
+                if (live_a) *(uint32_t *)Sa = wa[0];
+                if (live_b) *(uint32_t *)Sb = wb[0];
             } else {
-                uint32_t ka = kFull, kb = kFull;
-#pragma unroll
-                for (int j = 0; j < NR; j++) {
-                    const uint32_t d = (uint32_t)(lane * NR + j);
-                    ka = min(ka, ((tot[j] & 0xFFFFu) << 8) | d);
-                    kb = min(kb, ((tot[j] >> 16) << 8) | d);
-                }
-                da = __reduce_min_sync(kFull, ka) & 0xFFu;
-                db = __reduce_min_sync(kFull, kb) & 0xFFu;
+                if (live_a) *(uint2 *)Sa = make_uint2(wa[0], wa[1]);
+                if (live_b) *(uint2 *)Sb = make_uint2(wb[0], wb[1]);
             }
-            if (lane == 0) {
+            return;
+        }
+        // final passes: argmin over d, the lowest d winning ties; every lane reaches the reductions
+        uint32_t da, db;
+        if (KEY16) {
+            uint32_t k = kFull;
+#pragma unroll
+            for (int j = 0; j < NR; j++) k = vmin2(k, tot[j] * 64u + dpk[j]);       // S*64 + d (S <= 1016)
+            da = __reduce_min_sync(kFull, k & 0xFFFFu) & 0x3Fu;
+            db = (__reduce_min_sync(kFull, k) >> 16) & 0x3Fu;
+        } else {
+            uint32_t ka = kFull, kb = kFull;
+#pragma unroll
+            for (int j = 0; j < NR; j++) {
+                const uint32_t d = (uint32_t)(lane * NR + j);
+                ka = min(ka, ((tot[j] & 0xFFFFu) << 8) | d);
+                kb = min(kb, ((tot[j] >> 16) << 8) | d);
+            }
+            da = __reduce_min_sync(kFull, ka) & 0xFFu;
+            db = __reduce_min_sync(kFull, kb) & 0xFFu;
+        }
+        if (lane == 0) {
+            if (MODE == MODE_FINAL && P.even_only) {  // multi-scale: the map at (2x, 2y) only
+                if (live_a && !((xa | ya) & 1)) P.disp[(long long)(ya >> 1) * hw + (xa >> 1)] = (uint8_t)da;
+                if (live_b && !((xb | yb) & 1)) P.disp[(long long)(yb >> 1) * hw + (xb >> 1)] = (uint8_t)db;
+            } else {
                 if (live_a) P.disp[pa] = (uint8_t)da;
                 if (live_b) P.disp[pb] = (uint8_t)db;
             }
@@ -217,22 +301,32 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         __syncwarp();                                 // ... and every lane's; slot ch-1 is free
         issue(ch + NCH - 1);
         uint8_t *chunk = ring + (ch % NCH) * SLOT;
-        uint32_t c[K][NR], pl[K][3][NR];
+        uint32_t c[K][NR], pl[K][3][NR], sv[K][NR];
 #pragma unroll
         for (int k = 0; k < K; k++) {                 // the chunk's inputs, read before its steps run
             const uint8_t *r = chunk + k * SB + lane * NR;
             pair_unpack<NR>(ld_run<NR>(r), ld_run<NR>(r + D), c[k]);
-            if (MODE == MODE_FINAL3) {
 #pragma unroll
-                for (int q = 0; q < 3; q++) pair_unpack<NR>(ld_run<NR>(r + (q + 1) * 512), ld_run<NR>(r + (q + 1) * 512 + D), pl[k][q]);
+            for (int q = 0; q < NPL; q++)
+                pair_unpack<NR>(ld_run<NR>(r + (q + 1) * 512), ld_run<NR>(r + (q + 1) * 512 + D), pl[k][q]);
+            if (HAS_S) {
+                const uint8_t *sr = chunk + (1 + NPL) * 512 + k * 2 * SB + lane * 2 * NR;
+                uint32_t sa[NR > 1 ? NR / 2 : 1], sb[NR > 1 ? NR / 2 : 1];
+                if (NR == 1) { sa[0] = *(const uint16_t *)sr; sb[0] = *(const uint16_t *)(sr + 2 * D); }
+                else if (NR == 2) { sa[0] = *(const uint32_t *)sr; sb[0] = *(const uint32_t *)(sr + 2 * D); }
+                else {
+                    const uint2 a2 = *(const uint2 *)sr, b2 = *(const uint2 *)(sr + 2 * D);
+                    sa[0] = a2.x; sa[1] = a2.y; sb[0] = b2.x; sb[1] = b2.y;
+                }
+                pair_unpack16<NR>(sa, sb, sv[k]);
             }
         }
         if ((ch + 1) * K <= minlen) {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(c[k], pl[k], chunk + k * SB, ch * K + k, std::true_type{});
+            for (int k = 0; k < K; k++) step_once(c[k], pl[k], sv[k], chunk + k * SB, ch * K + k, std::true_type{});
         } else {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(c[k], pl[k], chunk + k * SB, ch * K + k, std::false_type{});
+            for (int k = 0; k < K; k++) step_once(c[k], pl[k], sv[k], chunk + k * SB, ch * K + k, std::false_type{});
         }
         if (MODE == MODE_SCRATCH) {
             __syncwarp();                             // every lane's L bytes of the chunk are staged

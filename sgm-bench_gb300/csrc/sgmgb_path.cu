@@ -13,49 +13,76 @@ k_path(const LineParams P) {
     path_warp<DPL, MODE, SAT, KEY16>(P, blockIdx.x * (blockDim.x >> 5) + wib, smem + wib * Slot<DPL, MODE>::RING);
 }
 
-template <int NR, int MODE, bool KEY16>
+template <int NR, int MODE, int SAT, bool KEY16>
 __global__ void __launch_bounds__(128)
 k_pair(const LineParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     const int wib = threadIdx.x >> 5;
-    path_pair<NR, MODE, KEY16>(P, blockIdx.x * (blockDim.x >> 5) + wib, smem + wib * PairSlot<NR, MODE>::RING);
+    path_pair<NR, MODE, SAT, KEY16>(P, blockIdx.x * (blockDim.x >> 5) + wib, smem + wib * PairSlot<NR, MODE>::RING);
 }
 
 // ---------------------------------------------------------------------------
-template <int NR, int MODE, bool KEY16>
+template <int NR, int MODE, int SAT, bool KEY16>
 static cudaError_t prep_pair() {
-    return cudaFuncSetAttribute(k_pair<NR, MODE, KEY16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_pair<NR, MODE, SAT, KEY16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 4 * PairSlot<NR, MODE>::RING);
 }
 
-template <int NR, int MODE, bool KEY16>
+template <int NR, int SAT>
+static cudaError_t prep_pair_modes() {
+    cudaError_t e;
+    if ((e = prep_pair<NR, MODE_SCRATCH, SAT, false>()) != cudaSuccess) return e;
+    if ((e = prep_pair<NR, MODE_STORE, SAT, false>()) != cudaSuccess) return e;
+    if ((e = prep_pair<NR, MODE_ACCUM, SAT, false>()) != cudaSuccess) return e;
+    return prep_pair<NR, MODE_FINAL, SAT, false>();
+}
+
+template <int NR, int MODE, int SAT, bool KEY16>
 static cudaError_t launch_pair_one(const LineParams &p, int wpb, cudaStream_t s) {
     const int warps = (p.nlines + 1) / 2;
     const dim3 b(32 * wpb), g((warps + wpb - 1) / wpb);
-    k_pair<NR, MODE, KEY16><<<g, b, wpb * PairSlot<NR, MODE>::RING, s>>>(p);
+    k_pair<NR, MODE, SAT, KEY16><<<g, b, wpb * PairSlot<NR, MODE>::RING, s>>>(p);
     return cudaGetLastError();
 }
 
 // The pair layout (two lines per warp in register halves, sgmgb_pair.cuh)
-// serves the scratch and 4-path final passes at D = 32, 64 and 128 unless a
-// disparities-per-lane shape was asked for.
+// serves the plain scratch and final-of-planes passes at D = 32, 64 and 128
+// unless a disparities-per-lane shape was asked for. (It runs every mode, with
+// saturation at D = 64, but when passes run one after another -- the sum
+// schedule -- their halved warp count costs more latency than the halved
+// instructions save; the batch kernel may still choose it for any mode.)
 static bool pair_applies(const LineParams &p, int mode, int saturate) {
-    return p.dpl == 0 && !saturate && (mode == MODE_SCRATCH || mode == MODE_FINAL3) &&
-           (p.D == 32 || p.D == 64 || p.D == 128);
+    return p.dpl == 0 && (p.D == 32 || p.D == 64 || p.D == 128) && !saturate &&
+           (mode == MODE_SCRATCH || mode == MODE_FINAL3);
 }
 
-static cudaError_t launch_pair(const LineParams &p, int mode, int wpb, cudaStream_t s) {
-    const bool key16 = p.key16 != 0;   // D <= 64 here
+template <int NR, int SAT>
+static cudaError_t launch_pair_nr(const LineParams &p, int mode, int wpb, cudaStream_t s) {
+    switch (mode) {
+    case MODE_SCRATCH: return launch_pair_one<NR, MODE_SCRATCH, SAT, false>(p, wpb, s);
+    case MODE_STORE:   return launch_pair_one<NR, MODE_STORE, SAT, false>(p, wpb, s);
+    case MODE_ACCUM:   return launch_pair_one<NR, MODE_ACCUM, SAT, false>(p, wpb, s);
+    case MODE_FINAL:   return launch_pair_one<NR, MODE_FINAL, SAT, false>(p, wpb, s);
+    default:           return cudaErrorInvalidValue;
+    }
+}
+
+static cudaError_t launch_pair(const LineParams &p, int mode, int saturate, int wpb, cudaStream_t s) {
+    if (saturate) return mode == MODE_FINAL3 ? cudaErrorInvalidValue : launch_pair_nr<2, 1>(p, mode, wpb, s);
+    const bool key16 = p.key16 != 0 && p.D <= 64;
+    if (mode == MODE_FINAL3) {
+        switch (p.D) {
+        case 32: return key16 ? launch_pair_one<1, MODE_FINAL3, 0, true>(p, wpb, s)
+                              : launch_pair_one<1, MODE_FINAL3, 0, false>(p, wpb, s);
+        case 64: return key16 ? launch_pair_one<2, MODE_FINAL3, 0, true>(p, wpb, s)
+                              : launch_pair_one<2, MODE_FINAL3, 0, false>(p, wpb, s);
+        default: return launch_pair_one<4, MODE_FINAL3, 0, false>(p, wpb, s);
+        }
+    }
     switch (p.D) {
-    case 32:
-        if (mode == MODE_SCRATCH) return launch_pair_one<1, MODE_SCRATCH, false>(p, wpb, s);
-        return key16 ? launch_pair_one<1, MODE_FINAL3, true>(p, wpb, s) : launch_pair_one<1, MODE_FINAL3, false>(p, wpb, s);
-    case 64:
-        if (mode == MODE_SCRATCH) return launch_pair_one<2, MODE_SCRATCH, false>(p, wpb, s);
-        return key16 ? launch_pair_one<2, MODE_FINAL3, true>(p, wpb, s) : launch_pair_one<2, MODE_FINAL3, false>(p, wpb, s);
-    default:
-        if (mode == MODE_SCRATCH) return launch_pair_one<4, MODE_SCRATCH, false>(p, wpb, s);
-        return launch_pair_one<4, MODE_FINAL3, false>(p, wpb, s);
+    case 32: return launch_pair_nr<1, 0>(p, mode, wpb, s);
+    case 64: return launch_pair_nr<2, 0>(p, mode, wpb, s);
+    default: return launch_pair_nr<4, 0>(p, mode, wpb, s);
     }
 }
 
@@ -77,14 +104,15 @@ static cudaError_t prep_dpl() {
 
 cudaError_t prepare_path_kernels() {
     cudaError_t e;
-    if ((e = prep_pair<1, MODE_SCRATCH, false>()) != cudaSuccess) return e;
-    if ((e = prep_pair<2, MODE_SCRATCH, false>()) != cudaSuccess) return e;
-    if ((e = prep_pair<4, MODE_SCRATCH, false>()) != cudaSuccess) return e;
-    if ((e = prep_pair<1, MODE_FINAL3, true>()) != cudaSuccess) return e;
-    if ((e = prep_pair<1, MODE_FINAL3, false>()) != cudaSuccess) return e;
-    if ((e = prep_pair<2, MODE_FINAL3, true>()) != cudaSuccess) return e;
-    if ((e = prep_pair<2, MODE_FINAL3, false>()) != cudaSuccess) return e;
-    if ((e = prep_pair<4, MODE_FINAL3, false>()) != cudaSuccess) return e;
+    if ((e = prep_pair_modes<1, 0>()) != cudaSuccess) return e;
+    if ((e = prep_pair_modes<2, 0>()) != cudaSuccess) return e;
+    if ((e = prep_pair_modes<4, 0>()) != cudaSuccess) return e;
+    if ((e = prep_pair_modes<2, 1>()) != cudaSuccess) return e;
+    if ((e = prep_pair<1, MODE_FINAL3, 0, true>()) != cudaSuccess) return e;
+    if ((e = prep_pair<1, MODE_FINAL3, 0, false>()) != cudaSuccess) return e;
+    if ((e = prep_pair<2, MODE_FINAL3, 0, true>()) != cudaSuccess) return e;
+    if ((e = prep_pair<2, MODE_FINAL3, 0, false>()) != cudaSuccess) return e;
+    if ((e = prep_pair<4, MODE_FINAL3, 0, false>()) != cudaSuccess) return e;
     if ((e = prep_dpl<2, 0, false>()) != cudaSuccess) return e;
     if ((e = prep_dpl<2, 0, true>()) != cudaSuccess) return e;
     if ((e = prep_dpl<4, 0, false>()) != cudaSuccess) return e;
@@ -124,10 +152,7 @@ int path_dpl(int D, int want) {
 cudaError_t launch_line(const LineParams &p0, int mode, int saturate, int warps_per_block, cudaStream_t s) {
     LineParams p = p0;
     if (warps_per_block < 1 || warps_per_block > 4 || p.nlines < 1 || !p.C) return cudaErrorInvalidValue;
-    if (pair_applies(p, mode, saturate)) {
-        p.key16 = p.key16 && p.D <= 64;
-        return launch_pair(p, mode, warps_per_block, s);
-    }
+    if (pair_applies(p, mode, saturate)) return launch_pair(p, mode, saturate, warps_per_block, s);
     const int dpl = path_dpl(p.D, p.dpl);
     if (!dpl || p.D % dpl) return cudaErrorInvalidValue;
     p.nl = p.D / dpl;                      // lanes per line that hold disparities
