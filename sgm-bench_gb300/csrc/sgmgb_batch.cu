@@ -5,7 +5,8 @@
 //   phase 1  cost     one item per band: C[p][d] from the band's census rows
 //   4 paths: phase 2  R->L, B->T, L->R into three u8 planes (all three passes)
 //            phase 3  T->B adds the planes to its L and takes the argmin
-//   8 paths: phase 2+k  pass k of the pair schedule (sc / S), k = 0..7
+//   8 paths: phase 2  R->L, L->R, B->T and the four diagonals into seven planes
+//            phase 3  T->B adds the seven planes to its L and takes the argmin
 // An item of phase k of frame f starts when every item of phase k-1 of f has
 // finished. Items are queued phase-major over all frames, so while one frame
 // waits at a phase boundary the others keep the SMs busy; every item's
@@ -29,7 +30,7 @@ namespace sgmgb {
 namespace {
 
 constexpr int BAND = tiles::CEN_ROWS;   // rows per census / cost item
-constexpr int MAXPH = 10;        // phases per frame (8 paths: census, cost, 8 passes)
+constexpr int MAXPH = 4;         // phases per frame: census, cost, scratch passes, final pass
 
 enum ItemKind : int { IT_CENSUS = 0, IT_COST = 1, IT_PATH = 2 };
 
@@ -139,6 +140,7 @@ __device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int wa
     case 2 * 8 + MODE_STORE:   path_warp<2, MODE_STORE, 0, false>(P, warp, ring); break;
     case 2 * 8 + MODE_ACCUM:   path_warp<2, MODE_ACCUM, 0, false>(P, warp, ring); break;
     case 2 * 8 + MODE_FINAL:   path_warp<2, MODE_FINAL, 0, false>(P, warp, ring); break;
+    case 2 * 8 + MODE_FINAL7:  path_warp<2, MODE_FINAL7, 0, false>(P, warp, ring); break;
     case 2 * 8 + MODE_FINAL3:
         if (key16) path_warp<2, MODE_FINAL3, 0, true>(P, warp, ring);
         else path_warp<2, MODE_FINAL3, 0, false>(P, warp, ring);
@@ -147,6 +149,7 @@ __device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int wa
     case 4 * 8 + MODE_STORE:   path_warp<4, MODE_STORE, 0, false>(P, warp, ring); break;
     case 4 * 8 + MODE_ACCUM:   path_warp<4, MODE_ACCUM, 0, false>(P, warp, ring); break;
     case 4 * 8 + MODE_FINAL:   path_warp<4, MODE_FINAL, 0, false>(P, warp, ring); break;
+    case 4 * 8 + MODE_FINAL7:  path_warp<4, MODE_FINAL7, 0, false>(P, warp, ring); break;
     case 4 * 8 + MODE_FINAL3:
         if (key16) path_warp<4, MODE_FINAL3, 0, true>(P, warp, ring);
         else path_warp<4, MODE_FINAL3, 0, false>(P, warp, ring);
@@ -155,6 +158,7 @@ __device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int wa
     case 8 * 8 + MODE_STORE:   path_warp<8, MODE_STORE, 0, false>(P, warp, ring); break;
     case 8 * 8 + MODE_ACCUM:   path_warp<8, MODE_ACCUM, 0, false>(P, warp, ring); break;
     case 8 * 8 + MODE_FINAL:   path_warp<8, MODE_FINAL, 0, false>(P, warp, ring); break;
+    case 8 * 8 + MODE_FINAL7:  path_warp<8, MODE_FINAL7, 0, false>(P, warp, ring); break;
     case 8 * 8 + MODE_FINAL3:  path_warp<8, MODE_FINAL3, 0, false>(P, warp, ring); break;
     default: break;
     }
@@ -226,16 +230,19 @@ int ring_bytes_for(int dpl, int mode) {
     case 2 * 8 + MODE_STORE:   return ring_of<2, MODE_STORE>();
     case 2 * 8 + MODE_ACCUM:   return ring_of<2, MODE_ACCUM>();
     case 2 * 8 + MODE_FINAL:   return ring_of<2, MODE_FINAL>();
+    case 2 * 8 + MODE_FINAL7:  return ring_of<2, MODE_FINAL7>();
     case 2 * 8 + MODE_FINAL3:  return ring_of<2, MODE_FINAL3>();
     case 4 * 8 + MODE_SCRATCH: return ring_of<4, MODE_SCRATCH>();
     case 4 * 8 + MODE_STORE:   return ring_of<4, MODE_STORE>();
     case 4 * 8 + MODE_ACCUM:   return ring_of<4, MODE_ACCUM>();
     case 4 * 8 + MODE_FINAL:   return ring_of<4, MODE_FINAL>();
+    case 4 * 8 + MODE_FINAL7:  return ring_of<4, MODE_FINAL7>();
     case 4 * 8 + MODE_FINAL3:  return ring_of<4, MODE_FINAL3>();
     case 8 * 8 + MODE_SCRATCH: return ring_of<8, MODE_SCRATCH>();
     case 8 * 8 + MODE_STORE:   return ring_of<8, MODE_STORE>();
     case 8 * 8 + MODE_ACCUM:   return ring_of<8, MODE_ACCUM>();
     case 8 * 8 + MODE_FINAL:   return ring_of<8, MODE_FINAL>();
+    case 8 * 8 + MODE_FINAL7:  return ring_of<8, MODE_FINAL7>();
     case 8 * 8 + MODE_FINAL3:  return ring_of<8, MODE_FINAL3>();
     default: return 0;
     }
@@ -321,6 +328,7 @@ int build_plan(sgmgb_batch *b) {
         base.nl = fd.D / dpl; base.lpl = base.nl; base.gpw = (32 % base.lpl == 0) ? 32 / base.lpl : 1;
         struct Spec { int dx, dy, mode, phase; uint8_t *sc; const uint8_t *sc2, *sc3; };
         std::vector<Spec> specs;
+        const uint8_t *xplanes[4] = {nullptr, nullptr, nullptr, nullptr};
         if (fd.paths == 4) {
             const size_t plane = (size_t)fd.W * fd.H * fd.D;
             uint8_t *pl[3] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane};
@@ -329,18 +337,23 @@ int build_plan(sgmgb_batch *b) {
             specs.push_back({1, 0, MODE_SCRATCH, 2, pl[2], nullptr, nullptr});
             specs.push_back({0, 1, MODE_FINAL3, 3, pl[0], pl[1], pl[2]});
         } else {
-            static const int sched[8][3] = {{-1, 0, MODE_SCRATCH}, {1, 0, MODE_STORE}, {0, -1, MODE_SCRATCH},
-                                            {0, 1, MODE_ACCUM}, {-1, -1, MODE_SCRATCH}, {1, 1, MODE_ACCUM},
-                                            {1, -1, MODE_SCRATCH}, {-1, 1, MODE_FINAL}};
-            for (int k = 0; k < 8; k++) specs.push_back({sched[k][0], sched[k][1], sched[k][2], 2 + k, s.sc, nullptr, nullptr});
+            // seven directions into seven planes, then T->B sums them (MODE_FINAL7)
+            const size_t plane = (size_t)fd.W * fd.H * fd.D;
+            uint8_t *pl[7] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane, s.xp, s.xp + plane, s.xp + 2 * plane,
+                              s.xp + 3 * plane};
+            static const int dirs[7][2] = {{-1, 0}, {1, 0}, {0, -1}, {-1, -1}, {1, 1}, {1, -1}, {-1, 1}};
+            for (int k = 0; k < 7; k++) specs.push_back({dirs[k][0], dirs[k][1], MODE_SCRATCH, 2, pl[k], nullptr, nullptr});
+            specs.push_back({0, 1, MODE_FINAL7, 3, pl[0], pl[1], pl[2]});
+            xplanes[0] = pl[3]; xplanes[1] = pl[4]; xplanes[2] = pl[5]; xplanes[3] = pl[6];
         }
         for (const Spec &sp : specs) {
             BPass bp{};
             bp.P = base;
             bp.P.dx = sp.dx; bp.P.dy = sp.dy;
             bp.P.sc = sp.sc; bp.P.sc2 = sp.sc2; bp.P.sc3 = sp.sc3;
+            for (int q = 0; q < 4; q++) bp.P.xpl[q] = xplanes[q];
             bp.P.nlines = lines_for(fd.W, fd.H, sp.dx, sp.dy);
-            const bool pair = fdpl == 0 && pair_ok(fd.D);
+            const bool pair = fdpl == 0 && pair_ok(fd.D) && sp.mode != MODE_FINAL7;
             bp.frame = f; bp.mode = sp.mode; bp.dpl = pair ? 0 : dpl;
             const int pi = (int)passes.size();
             passes.push_back(bp);

@@ -45,7 +45,8 @@ struct FrameSlot {
     uint8_t *C = nullptr;                                         // W*H*D cost volume
     uint8_t *C1 = nullptr;                                        // half-scale cost volume (multi-scale)
     uint8_t *sc = nullptr;                                        // W*H*D scratch L
-    uint16_t *S = nullptr;                                        // W*H*D sum
+    uint16_t *S = nullptr;                                        // W*H*D sum (or two u8 planes)
+    uint8_t *xp = nullptr;                                        // 8 paths: four more W*H*D u8 planes
     // multi-scale extras
     uint8_t *sobL = nullptr, *sobR = nullptr;                     // full-scale SobelX
     uint8_t *halfL = nullptr, *halfR = nullptr;                   // half-scale images
@@ -53,8 +54,9 @@ struct FrameSlot {
     uint64_t *cl1 = nullptr, *cr1 = nullptr;                      // half-scale census
     uint8_t *disp1 = nullptr;                                     // stage-1 argmin (defined work, unused)
     // independent path passes of one frame run on forked streams
-    cudaStream_t aux[2] = {nullptr, nullptr};
-    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+    static constexpr int kAux = 6;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t fork = nullptr, join[kAux] = {};
 };
 
 namespace sgmgb {

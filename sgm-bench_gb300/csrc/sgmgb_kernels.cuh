@@ -18,13 +18,15 @@ enum PassMode : int {
     MODE_STORE   = 1,   // S  = sc + L           (first pair: no memset of S)
     MODE_ACCUM   = 2,   // S += sc + L
     MODE_FINAL   = 3,   // argmin_d(S + sc + L) -> disp, lowest d on ties
-    MODE_FINAL3  = 4    // argmin_d(sc + sc2 + sc3 + L) -> disp: three other directions' planes
+    MODE_FINAL3  = 4,   // argmin_d(sc + sc2 + sc3 + L) -> disp: three other directions' planes
+    MODE_FINAL7  = 5    // argmin_d(L + the seven planes sc, sc2, sc3, xpl[0..3]) -> disp (8 paths)
 };
 
 struct LineParams {
     const uint8_t *C;            // cost volume at this scale, W*H*D
     uint8_t  *sc;                // W*H*D scratch L (written by SCRATCH, read otherwise)
-    const uint8_t *sc2, *sc3;    // MODE_FINAL3: the second and third planes
+    const uint8_t *sc2, *sc3;    // MODE_FINAL3 / FINAL7: the second and third planes
+    const uint8_t *xpl[4];       // MODE_FINAL7: planes four to seven
     uint16_t *S;                 // W*H*D sum
     uint8_t  *disp;              // final passes' output
     int W, H, D;
@@ -33,7 +35,7 @@ struct LineParams {
     int dx, dy;                  // direction of travel
     int p1, p2;                  // penalties
     int nlines;                  // independent lines for this direction
-    int even_only;               // final: argmin only at even (x,y) into a (W/2)x(H/2) map
+    int even_only;               // FINAL / FINAL7: argmin only at even (x,y) into a (W/2)x(H/2) map
     int key16;                   // final: S*64 + d fits 16 bits (4 paths, D <= 64)
     int dpl;                     // disparities per lane: 2, 4 or 8; 0 picks the smallest valid
 };

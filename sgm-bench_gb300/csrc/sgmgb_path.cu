@@ -99,6 +99,7 @@ static cudaError_t prep_dpl() {
     if ((e = prep_one<DPL, MODE_STORE, SAT, false>()) != cudaSuccess) return e;
     if ((e = prep_one<DPL, MODE_ACCUM, SAT, false>()) != cudaSuccess) return e;
     if ((e = prep_one<DPL, MODE_FINAL, SAT, false>()) != cudaSuccess) return e;
+    if ((e = prep_one<DPL, MODE_FINAL7, SAT, false>()) != cudaSuccess) return e;
     return prep_one<DPL, MODE_FINAL3, SAT, KEY16>();
 }
 
@@ -137,6 +138,8 @@ static cudaError_t launch_path_mode(const LineParams &p, int mode, dim3 g, dim3 
         k_path<DPL, MODE_FINAL, SAT, false><<<g, b, w * Slot<DPL, MODE_FINAL>::RING, s>>>(p); break;
     case MODE_FINAL3:
         k_path<DPL, MODE_FINAL3, SAT, KEY16><<<g, b, w * Slot<DPL, MODE_FINAL3>::RING, s>>>(p); break;
+    case MODE_FINAL7:
+        k_path<DPL, MODE_FINAL7, SAT, false><<<g, b, w * Slot<DPL, MODE_FINAL7>::RING, s>>>(p); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

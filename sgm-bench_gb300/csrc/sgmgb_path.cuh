@@ -89,7 +89,7 @@ __device__ __forceinline__ uint32_t group_min(uint32_t v, int G, int g, uint32_t
 }
 
 template <int MODE> struct Planes {   // scratch planes a pass reads
-    static constexpr int N = MODE == MODE_SCRATCH ? 0 : (MODE == MODE_FINAL3 ? 3 : 1);
+    static constexpr int N = MODE == MODE_SCRATCH ? 0 : (MODE == MODE_FINAL3 ? 3 : (MODE == MODE_FINAL7 ? 7 : 1));
 };
 
 // Ring geometry of a DPL. A step of one "byte stream" (the cost bytes or a
@@ -106,7 +106,10 @@ template <int DPL, int MODE> struct Slot {
     static constexpr bool HAS_S = MODE == MODE_ACCUM || MODE == MODE_FINAL;
     static constexpr int U = 1 + Planes<MODE>::N + (HAS_S ? 2 : 0);   // byte-stream units per step
     static constexpr int BYTES = Ring<DPL>::K * Ring<DPL>::SBM * U;  // one chunk of a warp
-    static constexpr int RING = Ring<DPL>::NCH * BYTES;               // a warp's whole ring
+    // ring depth: a chunk of eight streams (FINAL7) already carries 4 KB, so
+    // two chunks in flight keep as many bytes moving as deeper rings of one
+    static constexpr int NCH = U >= 8 ? 3 : Ring<DPL>::NCH;
+    static constexpr int RING = NCH * BYTES;                          // a warp's whole ring
 };
 
 template <int DPL, int MODE>
@@ -204,7 +207,8 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
         else tot[i] = __byte_perm(L[(2 * i) % NR] >> (16 * ((2 * i) / NR)),
                                   L[(2 * i + 1) % NR] >> (16 * ((2 * i + 1) / NR)), 0x5410);
         tot[i] += byte_pair(s.pw, i);
-        if (MODE == MODE_FINAL3) tot[i] += byte_pair(s.pw + SCW, i) + byte_pair(s.pw + 2 * SCW, i);
+#pragma unroll
+        for (int q = 1; q < Planes<MODE>::N; q++) tot[i] += byte_pair(s.pw + q * SCW, i);   // FINAL3, FINAL7
         if (MODE == MODE_ACCUM || MODE == MODE_FINAL) tot[i] += s.sw[i];   // no carry: S <= 2040
     }
     if (MODE == MODE_STORE || MODE == MODE_ACCUM) {
@@ -218,7 +222,8 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
     // final passes: argmin over d, the lowest d winning ties. Every lane of the
     // warp reaches group_min (it may reduce over the whole warp); a pixel that
     // is not kept (odd x or y of an even-only map) only skips the store.
-    const bool keep = live && !(MODE == MODE_FINAL && P.even_only && ((x | y) & 1));
+    constexpr bool EVEN = MODE == MODE_FINAL || MODE == MODE_FINAL7;   // modes with an even-only map
+    const bool keep = live && !(EVEN && P.even_only && ((x | y) & 1));
     uint32_t key;
     if (KEY16) {
         uint32_t k = kFull;
@@ -238,7 +243,7 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
     key = ONE ? __reduce_min_sync(kFull, key) : group_min(key, P.gpw, g, gmask);
     if (lead && keep) {
         const uint8_t d = (uint8_t)(KEY16 ? (key & 0x3Fu) : (key & 0xFFu));
-        if (MODE == MODE_FINAL && P.even_only) P.disp[(size_t)(y >> 1) * (P.W >> 1) + (x >> 1)] = d;
+        if (EVEN && P.even_only) P.disp[(size_t)(y >> 1) * (P.W >> 1) + (x >> 1)] = d;
         else P.disp[p] = d;
     }
 }
@@ -252,7 +257,7 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
 template <int DPL, int MODE, int SAT, bool KEY16>
 __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t *ring) {
     constexpr int NR = DPL / 2;
-    constexpr int K = Ring<DPL>::K, SBM = Ring<DPL>::SBM, NGB = Ring<DPL>::NGB, NCH = Ring<DPL>::NCH;
+    constexpr int K = Ring<DPL>::K, SBM = Ring<DPL>::SBM, NGB = Ring<DPL>::NGB, NCH = Slot<DPL, MODE>::NCH;
     constexpr int NPL = Planes<MODE>::N;
     constexpr bool HAS_S = Slot<DPL, MODE>::HAS_S;
     constexpr int SLOT = Slot<DPL, MODE>::BYTES;
@@ -328,7 +333,8 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
     }
     const uint8_t *pl[NPL > 0 ? NPL : 1];
     if (NPL > 0) pl[0] = P.sc;
-    if (NPL == 3) { pl[1] = P.sc2; pl[2] = P.sc3; }
+    if (NPL >= 3) { pl[1] = P.sc2; pl[2] = P.sc3; }
+    if (NPL == 7) { pl[3] = P.xpl[0]; pl[4] = P.xpl[1]; pl[5] = P.xpl[2]; pl[6] = P.xpl[3]; }
 
     // Enqueues chunk c (steps c*K .. c*K+K-1) into ring slot c % NCH.
     auto issue = [&](int c) {
@@ -448,6 +454,24 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
             __syncwarp();               // ... and every lane's; slot ch-1 is free
             issue(ch + NCH - 1);
             uint8_t *chunk = ring + (ch % NCH) * SLOT;
+            if (MODE == MODE_FINAL7) {  // eight input streams: read each step's inputs when it runs
+                if ((ch + 1) * K <= minlen) {
+#pragma unroll
+                    for (int k = 0; k < K; k++) {
+                        In s1;
+                        ring_read<DPL, MODE>(chunk, lane, k, s1);
+                        step_once(s1, ch * K + k, chunk + k * SBM + lane * DPL, std::true_type{}, one_t);
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < K; k++) {
+                        In s1;
+                        ring_read<DPL, MODE>(chunk, lane, k, s1);
+                        step_once(s1, ch * K + k, chunk + k * SBM + lane * DPL, std::false_type{}, one_t);
+                    }
+                }
+                continue;
+            }
             In s[K];                    // the chunk's inputs, read before its steps run
 #pragma unroll
             for (int k = 0; k < K; k++) ring_read<DPL, MODE>(chunk, lane, k, s[k]);

@@ -28,6 +28,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
     const size_t o_disp = take(out_n);
     const size_t o_cl = take(N * 8), o_cr = take(N * 8);
     const size_t o_C = take(N * D), o_sc = take(N * D), o_S = take(N * D * 2);
+    const size_t o_xp = fd.paths == 8 ? take(N * D * 4) : 0;
     size_t o_sobL = 0, o_sobR = 0, o_hL = 0, o_hR = 0, o_hsL = 0, o_hsR = 0, o_cl1 = 0, o_cr1 = 0, o_d1 = 0;
     size_t o_C1 = 0;
     if (fd.variant == SGMGB_MULTISCALE) {
@@ -43,6 +44,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
         s->left = b + o_left; s->right = b + o_right; s->disp = b + o_disp;
         s->cl = (uint64_t *)(b + o_cl); s->cr = (uint64_t *)(b + o_cr);
         s->C = b + o_C; s->sc = b + o_sc; s->S = (uint16_t *)(b + o_S);
+        if (fd.paths == 8) s->xp = b + o_xp;
         if (fd.variant == SGMGB_MULTISCALE) {
             s->C1 = b + o_C1;
             s->sobL = b + o_sobL; s->sobR = b + o_sobR;
@@ -67,9 +69,11 @@ int slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err) {
         return SGMGB_ERR_NOMEM;
     }
     slot_layout(fd, s);
-    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaStreamCreateWithFlags(&s->aux[i], cudaStreamNonBlocking);
+    for (int i = 0; i < FrameSlot::kAux && e == cudaSuccess; i++)
+        e = cudaStreamCreateWithFlags(&s->aux[i], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
-    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->join[i], cudaEventDisableTiming);
+    for (int i = 0; i < FrameSlot::kAux && e == cudaSuccess; i++)
+        e = cudaEventCreateWithFlags(&s->join[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         err = std::string("stream/event creation: ") + cudaGetErrorString(e);
         cudaGetLastError();
@@ -89,18 +93,11 @@ void slot_free(FrameSlot *s) {
     delete s;
 }
 
-// Pass schedule. Opposite directions are paired: the first of a pair parks
-// its L in the scratch plane, the second adds both into S; the last pass
-// also takes the argmin. Directions and penalties follow common/sgm_ref.c:
-// 96-99 (plain, P1 = 20 for all) and multiscale/sgm_ms_ref.c:85-87 (P1 40
-// horizontal, 20 vertical, 10 diagonal).
-struct PassSpec { int dx, dy, mode; };
-static const PassSpec kPasses4[4] = {
-    {-1, 0, MODE_SCRATCH}, {1, 0, MODE_STORE}, {0, -1, MODE_SCRATCH}, {0, 1, MODE_FINAL}};
-static const PassSpec kPasses8[8] = {
-    {-1, 0, MODE_SCRATCH}, {1, 0, MODE_STORE}, {0, -1, MODE_SCRATCH}, {0, 1, MODE_ACCUM},
-    {-1, -1, MODE_SCRATCH}, {1, 1, MODE_ACCUM}, {1, -1, MODE_SCRATCH}, {-1, 1, MODE_FINAL}};
-
+// Directions and penalties follow common/sgm_ref.c:96-99 (plain, P1 = 20 for
+// all) and multiscale/sgm_ms_ref.c:85-87 (P1 40 horizontal, 20 vertical, 10
+// diagonal). The sum over directions is order-independent, so the schedule is
+// this engine's: every direction but T->B parks its L in its own uint8 plane,
+// on forked streams, and T->B adds the planes to its own L and takes the argmin.
 static int ms_p1(int dx, int dy) { return dy == 0 ? 40 : (dx == 0 ? 20 : 10); }
 
 namespace {
@@ -129,32 +126,47 @@ const char *pass_name(int dx, int dy) {
     return dy > 0 ? "path_diag_tr_bl" : "path_diag_br_tl";
 }
 
-double mode_bytes(int mode, double ND, double N, double Nout) {
-    switch (mode) {
-    case MODE_SCRATCH: return 2 * ND;            // C in, plane out
-    case MODE_STORE:   return 4 * ND;            // C, sc in; S out
-    case MODE_ACCUM:   return 6 * ND;            // C, sc, S in; S out
-    case MODE_FINAL:   return 4 * ND + Nout;     // C, sc, S in; disp out
-    default:           return 4 * ND + Nout;     // FINAL3: C and three planes in; disp out
+// 8 paths at one scale: R->L, L->R, B->T and the four diagonals into seven
+// planes (sc, the two halves of S, four in xp), then T->B with MODE_FINAL7.
+// `serial` (a probe attached): all on `st`, one after another.
+cudaError_t run_planes8(const FrameSlot &s, const LineParams &base, int sat, bool ms, int wpb, cudaStream_t st,
+                        Marker &mark, double Nout) {
+    const bool serial = mark.pr != nullptr;
+    const size_t plane = (size_t)base.W * base.H * base.D;   // at this scale (fits the full-scale buffers)
+    const uint8_t *pl[7] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane, s.xp, s.xp + plane, s.xp + 2 * plane,
+                            s.xp + 3 * plane};
+    static const int dirs[7][2] = {{-1, 0}, {1, 0}, {0, -1}, {-1, -1}, {1, 1}, {1, -1}, {-1, 1}};
+    const double ND = (double)plane;
+    cudaStream_t ss[7];
+    for (int k = 0; k < 7; k++) ss[k] = (serial || k == 0) ? st : s.aux[k - 1];
+    cudaError_t e;
+    if (!serial) {
+        if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
+        for (int k = 1; k < 7; k++)
+            if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
     }
-}
-
-// Passes in order on one stream: each pair's first pass parks L in sc, its
-// second adds it into S (the pair schedule of the 8-path sum).
-cudaError_t run_paths(const LineParams &base, int paths, int sat, bool ms, int wpb, cudaStream_t st,
-                      Marker &mark, double Nout) {
-    const PassSpec *ps = paths == 8 ? kPasses8 : kPasses4;
-    const double ND = (double)base.W * base.H * base.D, N = (double)base.W * base.H;
-    for (int i = 0; i < paths; i++) {
-        LineParams p = base;
-        p.dx = ps[i].dx; p.dy = ps[i].dy;
-        p.p1 = ms ? ms_p1(p.dx, p.dy) : 20;
-        p.nlines = lines_for(p.W, p.H, p.dx, p.dy);
-        cudaError_t e = launch_line(p, ps[i].mode, sat, wpb, st);
-        if (e == cudaSuccess) e = mark(pass_name(p.dx, p.dy), mode_bytes(ps[i].mode, ND, N, Nout));
-        if (e != cudaSuccess) return e;
+    for (int k = 0; k < 7; k++) {
+        LineParams q = base;
+        q.dx = dirs[k][0]; q.dy = dirs[k][1]; q.sc = (uint8_t *)pl[k];
+        q.p1 = ms ? ms_p1(q.dx, q.dy) : 20;
+        q.nlines = lines_for(q.W, q.H, q.dx, q.dy);
+        if ((e = launch_line(q, MODE_SCRATCH, sat, wpb, ss[k])) != cudaSuccess) return e;
+        if ((e = mark(pass_name(q.dx, q.dy), 2 * ND)) != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    if (!serial) {
+        for (int k = 1; k < 7; k++) {
+            if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
+        }
+    }
+    LineParams q = base;
+    q.dx = 0; q.dy = 1;
+    q.sc = (uint8_t *)pl[0]; q.sc2 = pl[1]; q.sc3 = pl[2];
+    for (int k = 0; k < 4; k++) q.xpl[k] = pl[3 + k];
+    q.p1 = ms ? ms_p1(0, 1) : 20;
+    q.nlines = lines_for(q.W, q.H, 0, 1);
+    if ((e = launch_line(q, MODE_FINAL7, sat, wpb, st)) != cudaSuccess) return e;
+    return mark("path_tb_final", 8 * ND + Nout);
 }
 
 }  // namespace
@@ -181,7 +193,7 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         p.p2 = 192; p.even_only = 0; p.p1 = 20;
         p.key16 = (fd.paths == 4 && fd.D <= 64) ? 1 : 0;
         if (fd.paths == 8) {
-            if ((e = run_paths(p, fd.paths, 0, false, wpb, st, mark, N)) != cudaSuccess) return e;
+            if ((e = run_planes8(s, p, 0, false, wpb, st, mark, N)) != cudaSuccess) return e;
         } else {
             // 4 paths: R->L, B->T and L->R are independent; each parks its L in
             // a uint8 plane (the sum buffer's bytes hold planes 2 and 3) on its
@@ -239,12 +251,12 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         LineParams p1{};
         p1.C = s.C1; p1.sc = s.sc; p1.S = s.S; p1.disp = s.disp1;
         p1.W = hw; p1.H = hh; p1.D = 64; p1.dpl = shape.dpl; p1.p2 = 200; p1.even_only = 0;
-        if ((e = run_paths(p1, 8, 1, true, wpb, st, mark, Nh)) != cudaSuccess) return e;
+        if ((e = run_planes8(s, p1, 1, true, wpb, st, mark, Nh)) != cudaSuccess) return e;
         // stage 2: full scale, cost averaged with the half-scale cost (:183-199)
         LineParams p2{};
         p2.C = s.C; p2.sc = s.sc; p2.S = s.S; p2.disp = d_disp;
         p2.W = W; p2.H = H; p2.D = 64; p2.dpl = shape.dpl; p2.p2 = 200; p2.even_only = 1;
-        if ((e = run_paths(p2, 8, 1, true, wpb, st, mark, Nh)) != cudaSuccess) return e;
+        if ((e = run_planes8(s, p2, 1, true, wpb, st, mark, Nh)) != cudaSuccess) return e;
     }
     if (ev_end && (e = cudaEventRecord(ev_end, st)) != cudaSuccess) return e;
     return cudaSuccess;
