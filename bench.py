@@ -437,9 +437,11 @@ def run_gb300(args):
         for i in range(n):
             engines[i % nf].run_frame_async(dl[i % R], dr[i % R], dd[i % R], stream=streams[i % nf])
 
-    run_frames(args.warmup, NF)
+    # one frame at a time (a single context and stream, the latency schedule),
+    # for the frame latency
+    eng.set_schedule(sgmgb.SCHED_LATENCY)
+    run_frames(3, 1)
     torch.cuda.synchronize(dev)
-    # one frame at a time (a single context and stream), for the frame latency
     e0s, e1s = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     n_serial = max(10, args.steps // 4)
     e0s.record(s)
@@ -447,6 +449,9 @@ def run_gb300(args):
     e1s.record(s)
     torch.cuda.synchronize(dev)
     serial_ms_per_frame = e0s.elapsed_time(e1s) / n_serial
+    eng.set_schedule(sgmgb.SCHED_AUTO)   # frames in flight: the throughput schedule
+    run_frames(args.warmup, NF)
+    torch.cuda.synchronize(dev)
 
     def barrier():
         if dist is not None:
@@ -493,8 +498,13 @@ def run_gb300(args):
     e2e_value = replica_value(ws, e2e_steps, e2e_s)
     _, st = eng.run_frame(hl[0], hr[0], times=True)
 
-    # per-kernel device time, each kernel alone, CUDA events on the engine's stream
+    # per-kernel device time, each kernel alone, CUDA events on the engine's
+    # stream: the throughput schedule (`value`) and the latency one (`e2e`)
+    eng.set_schedule(sgmgb.SCHED_THROUGHPUT)
     kstats = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
+    eng.set_schedule(sgmgb.SCHED_LATENCY)
+    kstats_lat = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
+    eng.set_schedule(sgmgb.SCHED_AUTO)
 
     if rank != 0:
         for e in engines:
@@ -513,7 +523,7 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "u16", "data": "synthetic",
         "config": {"workload": WORKLOAD, "W": W, "H": H, "D": D, "paths": PATHS, "variant": "plain",
                    "inputs": "8 resident synthetic pairs round-robin; per-frame working set 570 MB > L2",
-                   "frames_in_flight": NF,
+                   "frames_in_flight": NF, "schedule": "throughput (frames in flight)",
                    "parallelism": "replicas" if ws > 1 else "single"},
         "frame_latency_ms": serial_ms_per_frame,
         "fps": ws * args.steps / (ms / 1e3),
@@ -521,11 +531,14 @@ def run_gb300(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * W * H, "d2h_bytes_per_step": W * H,
                 "fps": ws * e2e_steps / e2e_s, "p50_ms": statistics.median(lat) * 1e3,
                 "p99_ms": sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
-                "stage_ms": {k: round(v, 4) for k, v in st.items() if k.endswith("_ms")}},
+                "stage_ms": {k: round(v, 4) for k, v in st.items() if k.endswith("_ms")},
+                "schedule": "latency (one frame at a time)",
+                "kernels_alone_ms": {k[0]: round(k[1], 5) for k in kstats_lat}},
         "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": top[2],
                      "launch_ms": top[1],
-                     "note": "dominant kernel of the frame (longest mean launch, timed alone with CUDA events); "
+                     "note": "dominant kernel of the throughput-schedule frame (longest mean launch, timed alone "
+                             "with CUDA events); "
                              "achieved = its algorithmic bytes per launch / that time; peak = %s HBM copy "
                              "bandwidth; traffic = ncu dram bytes of one launch (profiles/)" % peak_kind},
         "frame_roofline": {"modelled_bytes": B_ALG, "achieved": B_ALG / (ms_per_step / 1e3) / 1e9,

@@ -23,6 +23,8 @@
  *   SGMGB_MULTISCALE plans the frame loop of the standalone multi-scale
  *                         binary (multiscale/sgm_ms_ref.c:166-202).
  *   sgmgb_profile_frame   no reference symbol: per-kernel timing for the bench.
+ *   sgmgb_set_path_shape, sgmgb_set_schedule
+ *                         no reference symbol: speed knobs, results unchanged.
  *   sgmgb_batch_*         no reference symbol: many frames per launch.
  *   sgmgb_server_*        no reference symbol: a continuous-batching request loop.
  */
@@ -95,6 +97,22 @@ int  sgmgb_plan(sgmgb_ctx *ctx, const sgmgb_frame_desc *fd);
  * not depend on it, only speed. Drops cached graphs. */
 int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane);
 
+/* Frame schedule (no reference symbol; results do not depend on it):
+ *   LATENCY     every direction parks its L in a uint8 plane, all directions
+ *               side by side, then one streaming pass adds the planes and
+ *               takes the argmin: the shortest frame when the GPU is idle;
+ *   THROUGHPUT  the last direction (T->B) adds the other directions' planes
+ *               to its own L and takes the argmin: one plane less written and
+ *               read per frame, for frames that share the GPU;
+ *   AUTO        LATENCY for sgmgb_run_frame and for a server frame with
+ *               nothing else in flight, THROUGHPUT for sgmgb_run_frame_async
+ *               and the other server frames (the default).
+ * Drops cached graphs. */
+#define SGMGB_SCHED_AUTO       0
+#define SGMGB_SCHED_LATENCY    1
+#define SGMGB_SCHED_THROUGHPUT 2
+int  sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule);
+
 /* ---- single frame ---- */
 /* Host buffers in and out, synchronous: the drop-in call. left/right are
  * W*H bytes, row-major; disp receives the output map (sgmgb_out_size). */
@@ -109,7 +127,7 @@ int sgmgb_sync(sgmgb_ctx *ctx, void *stream);
 
 /* ---- measurement (no reference symbol) ---- */
 typedef struct {
-    char   name[24];   /* "census", "cost", "path_rl", "path_tb_final", ... */
+    char   name[24];   /* "census", "cost", "path_rl", ..., "sum_argmin" */
     double ms;         /* mean device time of one launch (CUDA events) */
     double bytes;      /* algorithmic bytes of one launch: inputs read once, outputs written once */
 } sgmgb_kernel_stat;

@@ -106,8 +106,8 @@ __device__ void item_census(const BFrame &F, int band, uint8_t *sm) {
 __device__ void item_cost(const BFrame &F, int band, uint8_t *sm) {
     for (int y = band * BAND; y < min(band * BAND + BAND, F.H); y++)
         for (int x0 = 0; x0 < F.W; x0 += tiles::COST_PX)
-            tiles::cost_tile<true>(F.cl, F.cr, F.C, nullptr, F.W, F.D, kInvalidPlain, y, x0, sm, threadIdx.x,
-                                   blockDim.x);
+            tiles::cost_tile<true, false>(F.cl, F.cr, F.C, nullptr, F.W, F.D, kInvalidPlain, y, x0, sm,
+                                          threadIdx.x, blockDim.x);
 }
 
 // One warp's share of a path item: lines of warp `warp` of pass `bp`.

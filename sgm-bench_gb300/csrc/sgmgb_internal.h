@@ -8,11 +8,21 @@
 #include "sgmgb_kernels.cuh"
 
 // Shape of the path kernels: warps per block and disparities per lane
-// (0 = the smallest valid). Only speed depends on it.
+// (0 = the smallest valid), and the frame schedule (SGMGB_SCHED_*). Only
+// speed depends on them.
 struct PathShape {
     int wpb = 4;
     int dpl = 0;
+    int sched = SGMGB_SCHED_AUTO;
 };
+
+// The schedule a frame runs with. AUTO becomes LATENCY for a frame that has
+// the GPU to itself (the synchronous host-buffer call, a server frame with
+// nothing else in flight) and THROUGHPUT otherwise.
+inline PathShape resolve_sched(PathShape s, bool alone) {
+    if (s.sched == SGMGB_SCHED_AUTO) s.sched = alone ? SGMGB_SCHED_LATENCY : SGMGB_SCHED_THROUGHPUT;
+    return s;
+}
 
 struct sgmgb_ctx {
     int device = 0;
@@ -23,7 +33,7 @@ struct sgmgb_ctx {
     sgmgb_frame_desc fd{};
     bool planned = false;
     struct FrameSlot *slot = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // CUDA graphs of the planned frame pipeline, one per (left, right, disp)
     // pointer triple seen (a small round-robin cache); replayed by
     // sgmgb_run_frame_async, all dropped when the plan changes.
@@ -46,7 +56,7 @@ struct FrameSlot {
     uint8_t *C1 = nullptr;                                        // half-scale cost volume (multi-scale)
     uint8_t *sc = nullptr;                                        // W*H*D scratch L
     uint16_t *S = nullptr;                                        // W*H*D sum (or two u8 planes)
-    uint8_t *xp = nullptr;                                        // 8 paths: four more W*H*D u8 planes
+    uint8_t *xp = nullptr;                                        // 1 (4 paths) or 5 (8 paths) more W*H*D u8 planes
     // multi-scale extras
     uint8_t *sobL = nullptr, *sobR = nullptr;                     // full-scale SobelX
     uint8_t *halfL = nullptr, *halfR = nullptr;                   // half-scale images
@@ -54,7 +64,7 @@ struct FrameSlot {
     uint64_t *cl1 = nullptr, *cr1 = nullptr;                      // half-scale census
     uint8_t *disp1 = nullptr;                                     // stage-1 argmin (defined work, unused)
     // independent path passes of one frame run on forked streams
-    static constexpr int kAux = 6;
+    static constexpr int kAux = 7;
     cudaStream_t aux[kAux] = {};
     cudaEvent_t fork = nullptr, join[kAux] = {};
 };
@@ -69,7 +79,7 @@ void slot_free(FrameSlot *s);
 // Per-kernel timing of one enqueued frame: ev[0] before the first launch,
 // ev[i+1] after launch i (timing-enabled events, created by the caller).
 struct KernelProbe {
-    static constexpr int kMax = 24;
+    static constexpr int kMax = 32;
     int n = 0;
     cudaEvent_t ev[kMax + 1] = {};
     const char *name[kMax] = {};

@@ -56,12 +56,13 @@ __global__ void k_half2(const uint8_t *__restrict__ im0, const uint8_t *__restri
 // Cost volume of a frame at one scale, one row tile per block; the tile code
 // (and the cost definitions) are in sgmgb_tiles.cuh.
 // ---------------------------------------------------------------------------
+template <bool MS>
 __global__ void __launch_bounds__(256)
 k_cost(const uint64_t *__restrict__ cl, const uint64_t *__restrict__ cr, uint8_t *__restrict__ C,
        const uint8_t *__restrict__ C1, int W, int D, int invalid) {
     __shared__ __align__(16) uint8_t smem[tiles::COST_SMEM];
-    tiles::cost_tile<false>(cl, cr, C, C1, W, D, invalid, blockIdx.y, blockIdx.x * tiles::COST_PX, smem,
-                            threadIdx.x, 256);
+    tiles::cost_tile<false, MS>(cl, cr, C, C1, W, D, invalid, blockIdx.y, blockIdx.x * tiles::COST_PX, smem,
+                                threadIdx.x, 256);
 }
 
 // ---------------------------------------------------------------------------
@@ -71,7 +72,8 @@ cudaError_t launch_cost(const uint64_t *cl, const uint64_t *cr, uint8_t *C, cons
                         int W, int H, int D, int invalid, cudaStream_t s) {
     if (D < 16 || D > 256 || D % 16 || W < 1 || H < 1 || H > 65535) return cudaErrorInvalidValue;
     const dim3 g((W + tiles::COST_PX - 1) / tiles::COST_PX, H);
-    k_cost<<<g, 256, 0, s>>>(cl, cr, C, C1, W, D, invalid);
+    if (C1) k_cost<true><<<g, 256, 0, s>>>(cl, cr, C, C1, W, D, invalid);
+    else k_cost<false><<<g, 256, 0, s>>>(cl, cr, C, nullptr, W, D, invalid);
     return cudaGetLastError();
 }
 

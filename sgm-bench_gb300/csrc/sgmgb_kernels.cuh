@@ -71,4 +71,12 @@ cudaError_t prepare_path_kernels();
 // saturate: clamp L to 255 (multi-scale). warps_per_block in 1..4.
 cudaError_t launch_line(const LineParams &p, int mode, int saturate, int warps_per_block, cudaStream_t s);
 
+// Planes of one frame's directions, each W*H*D uint8 in the cost volume's
+// layout (16-byte aligned).
+struct SumPlanes { const uint8_t *p[8]; };
+// disp = argmin_d of the sum of the np (4 or 8) planes, lowest d on ties;
+// even_only: at even (x, y) only, into a (W/2)x(H/2) map (sgmgb_sum.cu).
+cudaError_t launch_sum(const SumPlanes &pl, int np, uint8_t *disp, int W, int H, int D, int even_only,
+                       cudaStream_t s);
+
 }  // namespace sgmgb

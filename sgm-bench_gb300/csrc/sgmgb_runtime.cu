@@ -1,7 +1,6 @@
 // sgmgb_runtime.cu -- context, resident workspace, frame pipeline and the
 // single-frame entry points of the C ABI (include/sgmgb.h).
 #include "sgmgb_internal.h"
-#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -28,7 +27,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
     const size_t o_disp = take(out_n);
     const size_t o_cl = take(N * 8), o_cr = take(N * 8);
     const size_t o_C = take(N * D), o_sc = take(N * D), o_S = take(N * D * 2);
-    const size_t o_xp = fd.paths == 8 ? take(N * D * 4) : 0;
+    const size_t o_xp = take(N * D * (fd.paths == 8 ? 5 : 1));
     size_t o_sobL = 0, o_sobR = 0, o_hL = 0, o_hR = 0, o_hsL = 0, o_hsR = 0, o_cl1 = 0, o_cr1 = 0, o_d1 = 0;
     size_t o_C1 = 0;
     if (fd.variant == SGMGB_MULTISCALE) {
@@ -44,7 +43,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
         s->left = b + o_left; s->right = b + o_right; s->disp = b + o_disp;
         s->cl = (uint64_t *)(b + o_cl); s->cr = (uint64_t *)(b + o_cr);
         s->C = b + o_C; s->sc = b + o_sc; s->S = (uint16_t *)(b + o_S);
-        if (fd.paths == 8) s->xp = b + o_xp;
+        s->xp = b + o_xp;
         if (fd.variant == SGMGB_MULTISCALE) {
             s->C1 = b + o_C1;
             s->sobL = b + o_sobL; s->sobR = b + o_sobR;
@@ -96,8 +95,9 @@ void slot_free(FrameSlot *s) {
 // Directions and penalties follow common/sgm_ref.c:96-99 (plain, P1 = 20 for
 // all) and multiscale/sgm_ms_ref.c:85-87 (P1 40 horizontal, 20 vertical, 10
 // diagonal). The sum over directions is order-independent, so the schedule is
-// this engine's: every direction but T->B parks its L in its own uint8 plane,
-// on forked streams, and T->B adds the planes to its own L and takes the argmin.
+// this engine's: every direction parks its L in its own uint8 plane, all of
+// them side by side on forked streams, and one streaming pass adds the planes
+// and takes the argmin.
 static int ms_p1(int dx, int dy) { return dy == 0 ? 40 : (dx == 0 ? 20 : 10); }
 
 namespace {
@@ -126,47 +126,104 @@ const char *pass_name(int dx, int dy) {
     return dy > 0 ? "path_diag_tr_bl" : "path_diag_br_tl";
 }
 
-// 8 paths at one scale: R->L, L->R, B->T and the four diagonals into seven
-// planes (sc, the two halves of S, four in xp), then T->B with MODE_FINAL7.
-// `serial` (a probe attached): all on `st`, one after another.
-cudaError_t run_planes8(const FrameSlot &s, const LineParams &base, int sat, bool ms, int wpb, cudaStream_t st,
-                        Marker &mark, double Nout) {
+// The THROUGHPUT schedule: every direction but T->B parks its L in its own
+// plane (the same planes as run_planes, one fewer), side by side on forked
+// streams; then T->B adds them to its own L and takes the argmin
+// (MODE_FINAL3 for 4 paths, MODE_FINAL7 for 8). One plane less is written
+// and read than with run_planes, at the price of a long pass on the frame's
+// critical path.
+cudaError_t run_final(const FrameSlot &s, const LineParams &base, int npaths, int sat, bool ms, int wpb,
+                      cudaStream_t st, Marker &mark, int even_only, uint8_t *disp, double Nout) {
     const bool serial = mark.pr != nullptr;
-    const size_t plane = (size_t)base.W * base.H * base.D;   // at this scale (fits the full-scale buffers)
-    const uint8_t *pl[7] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane, s.xp, s.xp + plane, s.xp + 2 * plane,
-                            s.xp + 3 * plane};
+    const size_t plane = (size_t)base.W * base.H * base.D;
+    uint8_t *pl[7] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane, s.xp, s.xp + plane, s.xp + 2 * plane,
+                      s.xp + 3 * plane};
     static const int dirs[7][2] = {{-1, 0}, {1, 0}, {0, -1}, {-1, -1}, {1, 1}, {1, -1}, {-1, 1}};
+    const int nsc = npaths - 1;
     const double ND = (double)plane;
     cudaStream_t ss[7];
-    for (int k = 0; k < 7; k++) ss[k] = (serial || k == 0) ? st : s.aux[k - 1];
+    for (int k = 0; k < nsc; k++) ss[k] = (serial || k == 0) ? st : s.aux[k - 1];
     cudaError_t e;
     if (!serial) {
         if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
-        for (int k = 1; k < 7; k++)
+        for (int k = 1; k < nsc; k++)
             if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
     }
-    for (int k = 0; k < 7; k++) {
+    for (int k = 0; k < nsc; k++) {
         LineParams q = base;
-        q.dx = dirs[k][0]; q.dy = dirs[k][1]; q.sc = (uint8_t *)pl[k];
+        q.dx = dirs[k][0]; q.dy = dirs[k][1]; q.sc = pl[k];
         q.p1 = ms ? ms_p1(q.dx, q.dy) : 20;
         q.nlines = lines_for(q.W, q.H, q.dx, q.dy);
         if ((e = launch_line(q, MODE_SCRATCH, sat, wpb, ss[k])) != cudaSuccess) return e;
         if ((e = mark(pass_name(q.dx, q.dy), 2 * ND)) != cudaSuccess) return e;
     }
     if (!serial) {
-        for (int k = 1; k < 7; k++) {
+        for (int k = 1; k < nsc; k++) {
             if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
         }
     }
     LineParams q = base;
     q.dx = 0; q.dy = 1;
-    q.sc = (uint8_t *)pl[0]; q.sc2 = pl[1]; q.sc3 = pl[2];
-    for (int k = 0; k < 4; k++) q.xpl[k] = pl[3 + k];
+    q.sc = pl[0]; q.sc2 = pl[1]; q.sc3 = pl[2];
+    for (int k = 0; k < 4; k++) q.xpl[k] = npaths == 8 ? pl[3 + k] : nullptr;
     q.p1 = ms ? ms_p1(0, 1) : 20;
     q.nlines = lines_for(q.W, q.H, 0, 1);
-    if ((e = launch_line(q, MODE_FINAL7, sat, wpb, st)) != cudaSuccess) return e;
-    return mark("path_tb_final", 8 * ND + Nout);
+    q.disp = disp;
+    q.even_only = even_only;
+    q.key16 = (npaths == 4 && base.D <= 64) ? 1 : 0;   // S*64 + d < 2^16
+    if ((e = launch_line(q, npaths == 8 ? MODE_FINAL7 : MODE_FINAL3, sat, wpb, st)) != cudaSuccess) return e;
+    return mark("path_tb_final", npaths * ND + Nout);
+}
+
+// The LATENCY schedule. Every direction (4 or 8 of them, at one scale)
+// parks its L in its own uint8 plane: sc, the two halves of S, then xp. The
+// directions run side by side on forked streams, longest (horizontal) first;
+// one pass then adds the planes and takes the argmin into `disp` (even_only:
+// the multi-scale full scale's (W/2)x(H/2) map). `serial` (a probe
+// attached): all on `st`, one after another.
+cudaError_t run_planes(const FrameSlot &s, const LineParams &base, int npaths, int sat, bool ms, int wpb,
+                       cudaStream_t st, Marker &mark, int even_only, uint8_t *disp, double Nout) {
+    const bool serial = mark.pr != nullptr;
+    const size_t plane = (size_t)base.W * base.H * base.D;   // at this scale (fits the full-scale buffers)
+    uint8_t *pl[8] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane, s.xp, s.xp + plane, s.xp + 2 * plane,
+                      s.xp + 3 * plane, s.xp + 4 * plane};
+    static const int dirs[8][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}, {-1, -1}, {1, 1}, {1, -1}, {-1, 1}};
+    const double ND = (double)plane;
+    cudaStream_t ss[8];
+    for (int k = 0; k < npaths; k++) ss[k] = (serial || k == 0) ? st : s.aux[k - 1];
+    cudaError_t e;
+    if (!serial) {
+        if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
+        for (int k = 1; k < npaths; k++)
+            if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
+    }
+    SumPlanes sp{};
+    for (int k = 0; k < npaths; k++) {
+        LineParams q = base;
+        q.dx = dirs[k][0]; q.dy = dirs[k][1]; q.sc = pl[k];
+        q.p1 = ms ? ms_p1(q.dx, q.dy) : 20;
+        q.nlines = lines_for(q.W, q.H, q.dx, q.dy);
+        sp.p[k] = pl[k];
+        if ((e = launch_line(q, MODE_SCRATCH, sat, wpb, ss[k])) != cudaSuccess) return e;
+        if ((e = mark(pass_name(q.dx, q.dy), 2 * ND)) != cudaSuccess) return e;
+    }
+    if (!serial) {
+        for (int k = 1; k < npaths; k++) {
+            if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
+        }
+    }
+    if ((e = launch_sum(sp, npaths, disp, base.W, base.H, base.D, even_only, st)) != cudaSuccess) return e;
+    const double Nsum = even_only ? Nout : (double)base.W * base.H;   // pixels whose planes are read
+    return mark("sum_argmin", npaths * Nsum * base.D + Nout);
+}
+
+cudaError_t run_dirs(const PathShape &shape, const FrameSlot &s, const LineParams &base, int npaths, int sat,
+                     bool ms, cudaStream_t st, Marker &mark, int even_only, uint8_t *disp, double Nout) {
+    if (shape.sched == SGMGB_SCHED_LATENCY)
+        return run_planes(s, base, npaths, sat, ms, shape.wpb, st, mark, even_only, disp, Nout);
+    return run_final(s, base, npaths, sat, ms, shape.wpb, st, mark, even_only, disp, Nout);
 }
 
 }  // namespace
@@ -175,7 +232,6 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
                           uint8_t *d_disp, cudaStream_t st, const PathShape &shape,
                           cudaEvent_t ev_census, cudaEvent_t ev_end, KernelProbe *probe) {
     const sgmgb_frame_desc &fd = s.fd;
-    const int wpb = shape.wpb;
     Marker mark{probe, st};
     const double N = (double)fd.W * fd.H, ND = N * fd.D;
     cudaError_t e;
@@ -191,42 +247,7 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         p.C = s.C; p.sc = s.sc; p.S = s.S; p.disp = d_disp;
         p.W = fd.W; p.H = fd.H; p.D = fd.D; p.dpl = shape.dpl;
         p.p2 = 192; p.even_only = 0; p.p1 = 20;
-        p.key16 = (fd.paths == 4 && fd.D <= 64) ? 1 : 0;
-        if (fd.paths == 8) {
-            if ((e = run_planes8(s, p, 0, false, wpb, st, mark, N)) != cudaSuccess) return e;
-        } else {
-            // 4 paths: R->L, B->T and L->R are independent; each parks its L in
-            // a uint8 plane (the sum buffer's bytes hold planes 2 and 3) on its
-            // own stream, then T->B adds all four and takes the argmin. With a
-            // probe attached they run one after another on `st`.
-            const size_t plane = (size_t)fd.W * fd.H * fd.D;
-            uint8_t *pl[3] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane};
-            const int dir[3][2] = {{-1, 0}, {0, -1}, {1, 0}};
-            cudaStream_t ss[3] = {st, probe ? st : s.aux[0], probe ? st : s.aux[1]};
-            if (!probe) {
-                if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
-                for (int k = 1; k < 3; k++)
-                    if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
-            }
-            for (int k = 0; k < 3; k++) {
-                LineParams q = p;
-                q.dx = dir[k][0]; q.dy = dir[k][1]; q.sc = pl[k];
-                q.nlines = lines_for(q.W, q.H, q.dx, q.dy);
-                if ((e = launch_line(q, MODE_SCRATCH, 0, wpb, ss[k])) != cudaSuccess) return e;
-                if ((e = mark(pass_name(q.dx, q.dy), 2 * ND)) != cudaSuccess) return e;
-            }
-            if (!probe) {
-                for (int k = 1; k < 3; k++) {
-                    if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
-                    if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
-                }
-            }
-            LineParams q = p;
-            q.dx = 0; q.dy = 1; q.sc = pl[0]; q.sc2 = pl[1]; q.sc3 = pl[2];
-            q.nlines = lines_for(q.W, q.H, 0, 1);
-            if ((e = launch_line(q, MODE_FINAL3, 0, wpb, st)) != cudaSuccess) return e;
-            if ((e = mark("path_tb_final", 4 * ND + N)) != cudaSuccess) return e;
-        }
+        if ((e = run_dirs(shape, s, p, fd.paths, 0, false, st, mark, 0, d_disp, N)) != cudaSuccess) return e;
     } else {
         const int W = fd.W, H = fd.H, hw = W / 2, hh = H / 2;
         const double Nh = (double)hw * hh, NhD = Nh * 64;
@@ -251,12 +272,12 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         LineParams p1{};
         p1.C = s.C1; p1.sc = s.sc; p1.S = s.S; p1.disp = s.disp1;
         p1.W = hw; p1.H = hh; p1.D = 64; p1.dpl = shape.dpl; p1.p2 = 200; p1.even_only = 0;
-        if ((e = run_planes8(s, p1, 1, true, wpb, st, mark, Nh)) != cudaSuccess) return e;
+        if ((e = run_dirs(shape, s, p1, 8, 1, true, st, mark, 0, s.disp1, Nh)) != cudaSuccess) return e;
         // stage 2: full scale, cost averaged with the half-scale cost (:183-199)
         LineParams p2{};
         p2.C = s.C; p2.sc = s.sc; p2.S = s.S; p2.disp = d_disp;
         p2.W = W; p2.H = H; p2.D = 64; p2.dpl = shape.dpl; p2.p2 = 200; p2.even_only = 1;
-        if ((e = run_planes8(s, p2, 1, true, wpb, st, mark, Nh)) != cudaSuccess) return e;
+        if ((e = run_dirs(shape, s, p2, 8, 1, true, st, mark, 1, d_disp, Nh)) != cudaSuccess) return e;
     }
     if (ev_end && (e = cudaEventRecord(ev_end, st)) != cudaSuccess) return e;
     return cudaSuccess;
@@ -334,7 +355,7 @@ int sgmgb_create(int device, sgmgb_ctx **out) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-    for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
+    for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
     if (e == cudaSuccess) e = prepare_path_kernels();
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -357,7 +378,8 @@ int sgmgb_profile_frame(sgmgb_ctx *ctx, const uint8_t *d_left, const uint8_t *d_
     int n = 0;
     for (int r = 0; r < reps && e == cudaSuccess; r++) {
         pr.n = 0;
-        e = enqueue_frame(*ctx->slot, d_left, d_right, d_disp, ctx->stream, ctx->shape, nullptr, nullptr, &pr);
+        e = enqueue_frame(*ctx->slot, d_left, d_right, d_disp, ctx->stream, resolve_sched(ctx->shape, true),
+                          nullptr, nullptr, &pr);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         for (int k = 0; k < pr.n && e == cudaSuccess; k++) {
             float ms = 0.f;
@@ -389,6 +411,17 @@ int sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane)
     drop_graph(ctx);
     ctx->shape.wpb = warps_per_block;
     ctx->shape.dpl = disp_per_lane;
+    return SGMGB_OK;
+}
+
+int sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule) {
+    if (!ctx) return SGMGB_ERR_ARG;
+    if (schedule != SGMGB_SCHED_AUTO && schedule != SGMGB_SCHED_LATENCY && schedule != SGMGB_SCHED_THROUGHPUT)
+        return set_err(ctx, SGMGB_ERR_ARG, "schedule must be SGMGB_SCHED_AUTO, _LATENCY or _THROUGHPUT");
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    ctx->shape.sched = schedule;
     return SGMGB_OK;
 }
 
@@ -439,32 +472,29 @@ int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right, u
     int ow = 0, oh = 0;
     sgmgb_out_size(&s.fd, &ow, &oh);
     const size_t outN = (size_t)ow * oh;
-    using clk = std::chrono::steady_clock;
-    const auto tA = clk::now();
-    cudaError_t e = cudaMemcpyAsync(s.left, left, N, cudaMemcpyHostToDevice, ctx->stream);
+    // copies in, the frame, the copy out: one stream, one wait at the end
+    cudaEvent_t *ev = ctx->ev;   // 0 start, 3 inputs in, 1 census and cost done, 2 frame done, 4 map out
+    cudaError_t e = cudaEventRecord(ev[0], ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s.left, left, N, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s.right, right, N, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "host-to-device copy");
-    const auto tB = clk::now();
-    e = cudaEventRecord(ctx->ev[0], ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3], ctx->stream);
     if (e == cudaSuccess)
-        e = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, ctx->shape, ctx->ev[1], ctx->ev[2]);
+        e = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, resolve_sched(ctx->shape, true), ev[1], ev[2]);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(disp, s.disp, outN, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[4], ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "frame pipeline");
-    const auto tC = clk::now();
-    e = cudaMemcpyAsync(disp, s.disp, outN, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "device-to-host copy");
-    const auto tD = clk::now();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "frame (copies and pipeline)");
     if (t) {
-        float census = 0, agg = 0;
-        cudaEventElapsedTime(&census, ctx->ev[0], ctx->ev[1]);
-        cudaEventElapsedTime(&agg, ctx->ev[1], ctx->ev[2]);
+        float census = 0, agg = 0, in = 0, out = 0;
+        cudaEventElapsedTime(&census, ev[3], ev[1]);
+        cudaEventElapsedTime(&agg, ev[1], ev[2]);
+        cudaEventElapsedTime(&in, ev[0], ev[3]);
+        cudaEventElapsedTime(&out, ev[2], ev[4]);
         t->census_ms = census;
         t->cost_ms = -1;
         t->aggregate_ms = agg;
         t->argmin_ms = -1;
-        t->transfer_ms = std::chrono::duration<double, std::milli>((tB - tA) + (tD - tC)).count();
+        t->transfer_ms = (double)in + out;
         t->threads_used = 0;
     }
     return SGMGB_OK;
@@ -486,7 +516,8 @@ static cudaError_t capture_frame_graph(sgmgb_ctx *ctx, const uint8_t *l, const u
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    cudaError_t ee = enqueue_frame(*ctx->slot, l, r, d, ctx->stream, ctx->shape, nullptr, nullptr);
+    cudaError_t ee = enqueue_frame(*ctx->slot, l, r, d, ctx->stream, resolve_sched(ctx->shape, false), nullptr,
+                                   nullptr);
     e = cudaStreamEndCapture(ctx->stream, &g);
     if (ee != cudaSuccess) { if (g) cudaGraphDestroy(g); return ee; }
     if (e != cudaSuccess) return e;

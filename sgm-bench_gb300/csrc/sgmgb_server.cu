@@ -133,15 +133,18 @@ bool make_slot(const sgmgb_frame_desc &fd, Slot *out) {
     return true;
 }
 
-// Enqueues request r on slot k of its camera (no lock held).
-bool launch(sgmgb_server *s, Request *r, int k, std::string &err) {
+// Enqueues request r on slot k of its camera (no lock held). `alone`: the
+// frame was admitted with nothing else in flight (the latency schedule under
+// SGMGB_SCHED_AUTO).
+bool launch(sgmgb_server *s, Request *r, int k, bool alone, std::string &err) {
     Camera *c = r->cam;
     Slot &sl = c->slots[k];
     const FrameSlot &fs = *sl.fs;
     uint8_t *hb = c->bufs[r->buf];
     cudaError_t e = cudaMemcpyAsync(fs.left, hb, c->n_in, cudaMemcpyHostToDevice, sl.st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fs.right, hb + c->n_in, c->n_in, cudaMemcpyHostToDevice, sl.st);
-    if (e == cudaSuccess) e = enqueue_frame(fs, fs.left, fs.right, fs.disp, sl.st, s->ctx->shape, nullptr, nullptr);
+    if (e == cudaSuccess)
+        e = enqueue_frame(fs, fs.left, fs.right, fs.disp, sl.st, resolve_sched(s->ctx->shape, alone), nullptr, nullptr);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hb + 2 * c->n_in, fs.disp, c->n_out, cudaMemcpyDeviceToHost, sl.st);
     if (e == cudaSuccess) e = cudaLaunchHostFunc(sl.st, on_frame_done, r);
     if (e != cudaSuccess) {
@@ -156,6 +159,7 @@ struct Admission {
     Request *r;
     int slot;        // -1: a new slot is to be made for it
     size_t grow;     // bytes reserved for that slot
+    bool alone;      // nothing else in flight when it was admitted
 };
 
 // Picks queued requests for free slots, oldest head first over the cameras,
@@ -183,8 +187,9 @@ std::vector<Admission> plan_admissions(sgmgb_server *s) {
         if (pick_k >= 0) pick->slots[pick_k].busy = true;
         else { pick->growing++; s->resident += pick_grow; }
         r->state = 1;
+        const bool alone = s->inflight == 0;
         s->inflight++;
-        out.push_back({r, pick_k, pick_grow});
+        out.push_back({r, pick_k, pick_grow, alone});
     }
     return out;
 }
@@ -228,7 +233,7 @@ void worker_main(sgmgb_server *s) {
                 grown.push_back({c, a.grow});
             }
             a.r->slot = a.slot;
-            if (!launch(s, a.r, a.slot, err)) failed.push_back({a, err});
+            if (!launch(s, a.r, a.slot, a.alone, err)) failed.push_back({a, err});
         }
         lk.lock();
         for (auto &g : grown) g.first->growing--;

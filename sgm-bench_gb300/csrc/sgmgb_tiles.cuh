@@ -123,7 +123,47 @@ __device__ __forceinline__ uint64_t ld_desc(const uint64_t *p) {
     return LD_CG ? __ldcg(p) : __ldg(p);
 }
 
-template <bool LD_CG>
+// One pixel's 8 costs d0..d0+7 from staged descriptors; r[-k] = cr[x - d0 - k].
+// EDGE: some x - d0 - k may be negative (the first D columns of a row).
+template <bool EDGE>
+__device__ __forceinline__ void cost8(uint64_t a, const uint64_t *r, int x, int d0, int invalid, uint32_t (&v)[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint32_t c = (uint32_t)__popcll(a ^ r[-k]);
+        v[k] = EDGE && x - d0 - k < 0 ? (uint32_t)invalid : c;
+    }
+}
+
+// The tile's compute loop. DG4: D/8 a multiple of 4 (a warp covers 8 pixels x 4
+// groups of 8 disparities; otherwise 16 x 2). MS: average with the half-scale
+// cost. EDGE / TAIL: the tile has columns x < D - 1 / columns past W.
+template <bool DG4, bool MS, bool EDGE, bool TAIL>
+__device__ __forceinline__ void cost_tasks(const uint64_t *sl, const uint64_t *sr, uint8_t *__restrict__ row,
+                                           const uint8_t *__restrict__ C1, int W, int D, int invalid, int y,
+                                           int x0, int tid, int nthreads) {
+    constexpr int DG = DG4 ? 4 : 2, PXW = 32 / DG, LNXB = DG4 ? 3 : 2;   // LNXB = log2(COST_PX / PXW)
+    const int lane = tid & 31;
+    const int pxl = lane / DG, dgl = lane & (DG - 1);
+    const int ntask = ((D >> 3) / DG) << LNXB;
+    const int hw = W >> 1;
+    for (int task = tid >> 5; task < ntask; task += nthreads >> 5) {
+        const int dgb = task >> LNXB, px = (task & ((1 << LNXB) - 1)) * PXW + pxl;
+        const int d0 = (dgb * DG + dgl) * 8, x = x0 + px;
+        if (TAIL && x >= W) continue;
+        uint32_t v[8];
+        cost8<EDGE>(sl[px], sr + px + (D - 1) - d0, x, d0, invalid, v);
+        if (MS) {   // full scale of the multi-scale variant
+            const uint32_t h = *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + (x >> 1)) * D + (d0 >> 1));
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = (v[k] + ((h >> (8 * (k >> 1))) & 0xFFu) + 1) >> 1;
+        }
+        const uint32_t lo = v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24);
+        const uint32_t hi = v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24);
+        *(uint2 *)(row + (size_t)x * D + d0) = make_uint2(lo, hi);
+    }
+}
+
+template <bool LD_CG, bool MS>
 __device__ __forceinline__ void cost_tile(const uint64_t *__restrict__ cl, const uint64_t *__restrict__ cr,
                                           uint8_t *__restrict__ C, const uint8_t *__restrict__ C1, int W,
                                           int D, int invalid, int y, int x0, uint8_t *smem, int tid,
@@ -141,37 +181,15 @@ __device__ __forceinline__ void cost_tile(const uint64_t *__restrict__ cl, const
         }
     }
     __syncthreads();
-    const int tpp = D >> 3;                           // disparity groups of 8 per pixel
-    const int DG = (tpp & 3) ? 2 : 4, PXW = 32 / DG;
-    const int lane = tid & 31;
-    const int pxl = DG == 4 ? lane >> 2 : lane >> 1, dgl = lane & (DG - 1);
-    const int lnxb = DG == 4 ? 3 : 2;                 // log2(COST_PX / PXW)
-    const int ntask = (tpp / DG) << lnxb;
-    const int hw = W >> 1;
     uint8_t *row = C + (size_t)y * W * D;
-    for (int task = tid >> 5; task < ntask; task += nthreads >> 5) {
-        const int dgb = task >> lnxb, px = (task & ((1 << lnxb) - 1)) * PXW + pxl;
-        const int d0 = (dgb * DG + dgl) * 8, x = x0 + px;
-        if (x >= W) continue;
-        const uint64_t a = sl[px];
-        const uint64_t *r = sr + px + (D - 1) - d0;   // r[-k] = cr[x - d0 - k]
-        uint32_t v[8];
-        if (x >= d0 + 7) {
-#pragma unroll
-            for (int k = 0; k < 8; k++) v[k] = (uint32_t)__popcll(a ^ r[-k]);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 8; k++) v[k] = x - d0 - k >= 0 ? (uint32_t)__popcll(a ^ r[-k]) : (uint32_t)invalid;
-        }
-        if (C1) {   // full scale of the multi-scale variant
-            const uint32_t h = *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + (x >> 1)) * D + (d0 >> 1));
-#pragma unroll
-            for (int k = 0; k < 8; k++) v[k] = (v[k] + ((h >> (8 * (k >> 1))) & 0xFFu) + 1) >> 1;
-        }
-        const uint32_t lo = v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24);
-        const uint32_t hi = v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24);
-        *(uint2 *)(row + (size_t)x * D + d0) = make_uint2(lo, hi);
-    }
+    const bool dg4 = ((D >> 3) & 3) == 0;
+    const bool edge = x0 < D - 1, tail = x0 + COST_PX > W;   // uniform over the block
+    if (dg4 && !edge && !tail)
+        cost_tasks<true, MS, false, false>(sl, sr, row, C1, W, D, invalid, y, x0, tid, nthreads);
+    else if (dg4)
+        cost_tasks<true, MS, true, true>(sl, sr, row, C1, W, D, invalid, y, x0, tid, nthreads);
+    else
+        cost_tasks<false, MS, true, true>(sl, sr, row, C1, W, D, invalid, y, x0, tid, nthreads);
     __syncthreads();                                  // the tile memory may be reused next
 }
 

@@ -20,13 +20,14 @@ BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD, "libsgmgb.so")
 
 PLAIN, MULTISCALE = 0, 1
+SCHED_AUTO, SCHED_LATENCY, SCHED_THROUGHPUT = 0, 1, 2
 OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_NODEV, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 
 # every symbol include/sgmgb.h declares
 EXPORTS = [
     "sgmgb_abi_version", "sgmgb_strerror", "sgmgb_last_error", "sgmgb_check_desc", "sgmgb_out_size",
     "sgmgb_workspace_bytes", "sgmgb_create", "sgmgb_destroy", "sgmgb_plan", "sgmgb_set_path_shape",
-    "sgmgb_profile_frame",
+    "sgmgb_set_schedule", "sgmgb_profile_frame",
     "sgmgb_run_frame",
     "sgmgb_run_frame_async", "sgmgb_sync", "sgmgb_census_async", "sgmgb_batch_create", "sgmgb_batch_run",
     "sgmgb_batch_wait", "sgmgb_batch_autotune", "sgmgb_batch_tile_shape", "sgmgb_batch_set_fault",
@@ -89,6 +90,7 @@ def _load():
         "sgmgb_destroy": (None, [vp]),
         "sgmgb_plan": (i, [vp, fdp]),
         "sgmgb_set_path_shape": (i, [vp, i, i]),
+        "sgmgb_set_schedule": (i, [vp, i]),
         "sgmgb_profile_frame": (i, [vp, u8p, u8p, u8p, i, ctypes.POINTER(KernelStat), i, ctypes.POINTER(i)]),
         "sgmgb_run_frame": (i, [vp, u8p, u8p, u8p, ctypes.POINTER(StageTimes)]),
         "sgmgb_run_frame_async": (i, [vp, u8p, u8p, u8p, vp]),
@@ -232,6 +234,12 @@ class Engine:
     def set_path_shape(self, warps_per_block=4, disp_per_lane=0):
         """Path-kernel shape (speed only; results are identical)."""
         self._check(lib.sgmgb_set_path_shape(self.h, warps_per_block, disp_per_lane))
+        return self
+
+    def set_schedule(self, schedule=SCHED_AUTO):
+        """Frame schedule: SCHED_LATENCY, SCHED_THROUGHPUT or SCHED_AUTO (speed
+        only; results are identical)."""
+        self._check(lib.sgmgb_set_schedule(self.h, schedule))
         return self
 
     def profile_frame(self, d_left, d_right, d_disp, reps=10):

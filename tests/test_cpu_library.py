@@ -64,8 +64,8 @@ def test_out_size_and_workspace():
     assert sgmgb.out_size(1920, 800, 64, 8, sgmgb.MULTISCALE) == (960, 400)
     small, big = sgmgb.workspace_bytes(640, 480, 64, 4), sgmgb.workspace_bytes(1920, 1080, 64, 4)
     N = 1920 * 1080
-    assert big >= N * 64 * 4 + 16 * N                 # cost volume, scratch and sum planes, census
-    assert big < N * 64 * 4 + 24 * N + (1 << 16)
+    assert big >= N * 64 * 5 + 16 * N                 # cost volume, four direction planes, census
+    assert big < N * 64 * 5 + 24 * N + (1 << 16)
     assert small < big
     assert sgmgb.workspace_bytes(1920, 1080, 128, 4) > big
     with pytest.raises(sgmgb.SgmError):

@@ -201,15 +201,60 @@ def test_profile_frame_lists_every_kernel(engine):
     left, right, _ = sgmgb.synth_pair(W, H, 64, seed=3)
     dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
     dd = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
-    engine.plan(W, H, 64, 4)
-    stats = engine.profile_frame(dl, dr, dd, reps=3)
-    assert [s[0] for s in stats] == ["census", "cost", "path_rl", "path_bt", "path_lr", "path_tb_final"]
-    assert all(ms > 0 and b > 0 for _, ms, b in stats)
-    assert stats[-1][2] == 4 * W * H * 64 + W * H
-    assert np.array_equal(dd.cpu().numpy(), oracle.plain(left, right, 64, 4))   # the timed frames are real frames
-    engine.plan(W, H, 64, 8, sgmgb.MULTISCALE)
-    dd2 = torch.zeros((H // 2, W // 2), dtype=torch.uint8, device="cuda")
-    names = [s[0] for s in engine.profile_frame(dl, dr, dd2, reps=2)]
-    assert names[:7] == ["half", "sobel_half", "census_half", "cost_half", "sobel", "census", "cost_merge"]
-    assert len(names) == 7 + 16
-    assert np.array_equal(dd2.cpu().numpy(), oracle.multiscale(left, right))
+    want = oracle.plain(left, right, 64, 4)
+    want_ms = oracle.multiscale(left, right)
+    dirs4 = ["census", "cost", "path_rl", "path_lr", "path_bt"]
+    cases = [(sgmgb.SCHED_AUTO, dirs4 + ["path_tb", "sum_argmin"], 9),       # a synchronous call: latency
+             (sgmgb.SCHED_LATENCY, dirs4 + ["path_tb", "sum_argmin"], 9),
+             (sgmgb.SCHED_THROUGHPUT, dirs4 + ["path_tb_final"], 8)]
+    try:
+        for sched, names4, per_scale in cases:
+            engine.set_schedule(sched)
+            engine.plan(W, H, 64, 4)
+            dd.zero_()
+            stats = engine.profile_frame(dl, dr, dd, reps=3)
+            assert [s[0] for s in stats] == names4
+            assert all(ms > 0 and b > 0 for _, ms, b in stats)
+            assert stats[-1][2] == 4 * W * H * 64 + W * H
+            assert np.array_equal(dd.cpu().numpy(), want)   # the timed frames are real frames
+            engine.plan(W, H, 64, 8, sgmgb.MULTISCALE)
+            dd2 = torch.zeros((H // 2, W // 2), dtype=torch.uint8, device="cuda")
+            names = [s[0] for s in engine.profile_frame(dl, dr, dd2, reps=2)]
+            assert names[:7] == ["half", "sobel_half", "census_half", "cost_half", "sobel", "census", "cost_merge"]
+            assert len(names) == 7 + 2 * per_scale and names[-1] == names4[-1]
+            assert np.array_equal(dd2.cpu().numpy(), want_ms)
+    finally:
+        engine.set_schedule(sgmgb.SCHED_AUTO)
+
+
+@pytest.mark.parametrize("sched", ["latency", "throughput"])
+def test_schedules_agree(engine, sched):
+    """Both frame schedules, through the host-buffer call and the device-buffer
+    call, on the shapes that take the sum pass's other code paths (D/16 not a
+    divisor of 32, 32-bit keys, 8 planes, even-only)."""
+    import torch
+    engine.set_schedule(sgmgb.SCHED_LATENCY if sched == "latency" else sgmgb.SCHED_THROUGHPUT)
+    try:
+        for (W, H, D, paths) in [(300, 70, 48, 4), (301, 71, 128, 4), (160, 90, 32, 8), (200, 64, 64, 8),
+                                 (97, 33, 80, 8)]:
+            left, right, _ = sgmgb.synth_pair(W, H, min(D, 128), seed=W + D)
+            want = oracle.plain(left, right, D, paths)
+            engine.plan(W, H, D, paths)
+            assert np.array_equal(engine.run_frame(left, right), want), (W, H, D, paths)
+            dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
+            dd = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+            engine.run_frame_async(dl, dr, dd)
+            engine.sync()
+            assert np.array_equal(dd.cpu().numpy(), want), (W, H, D, paths, "async")
+        left, right, _ = sgmgb.synth_pair(130, 66, 64, seed=5)
+        engine.plan(130, 66, 64, 8, sgmgb.MULTISCALE)
+        assert np.array_equal(engine.run_frame(left, right), oracle.multiscale(left, right))
+    finally:
+        engine.set_schedule(sgmgb.SCHED_AUTO)
+
+
+def test_rejects_bad_schedule(engine):
+    with pytest.raises(sgmgb.SgmError):
+        engine.set_schedule(3)
+    with pytest.raises(sgmgb.SgmError):
+        engine.set_schedule(-1)
