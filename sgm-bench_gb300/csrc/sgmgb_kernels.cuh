@@ -35,7 +35,9 @@ struct LineParams {
     int dx, dy;                  // direction of travel
     int p1, p2;                  // penalties
     int nlines;                  // independent lines for this direction
-    int even_only;               // FINAL / FINAL7: argmin only at even (x,y) into a (W/2)x(H/2) map
+    int even_only;               // multi-scale full scale: only lines through even (x, y) (nlines from
+                                 // lines_for_even), SCRATCH stores and final argmins only at even (x, y),
+                                 // the map (W/2)x(H/2)
     int key16;                   // final: S*64 + d fits 16 bits (4 paths, D <= 64)
     int dpl;                     // disparities per lane: 2, 4 or 8; 0 picks the smallest valid
 };
@@ -51,6 +53,19 @@ inline int lines_for(int W, int H, int dx, int dy) {
     if (dy == 0) return H;
     if (dx == 0) return W;
     return W + H - 1;
+}
+
+// The same with LineParams::even_only (W and H even): the lines that cross a
+// pixel with x and y both even -- even rows, even columns, or the diagonals
+// with x + y even, counted over the entry rows and then the entry columns.
+inline int lines_for_even(int W, int H, int dx, int dy) {
+    if (dy == 0) return (H + 1) / 2;
+    if (dx == 0) return (W + 1) / 2;
+    const int xe = dx > 0 ? 0 : W - 1, ye = dy > 0 ? 0 : H - 1;
+    const int n1 = (H - (xe & 1) + 1) / 2;
+    const int m0 = ((xe + ye) & 1) ? 1 : 2;          // first entry column offset with xe + m + ye even
+    const int n2 = W - 1 >= m0 ? (W - 1 - m0) / 2 + 1 : 0;
+    return n1 + n2;
 }
 
 // ---- launchers (all enqueue on `s`, none synchronises) ----

@@ -113,20 +113,6 @@ __device__ __forceinline__ void st_run(uint8_t *p, uint32_t v) {
     else *(uint32_t *)p = v;
 }
 
-// Entry pixel and length of `line` of direction (dx, dy).
-__device__ __forceinline__ void line_geo(const LineParams &P, int line, int &x, int &y, int &len) {
-    const int dx = P.dx, dy = P.dy;
-    const int xe = dx > 0 ? 0 : P.W - 1, ye = dy > 0 ? 0 : P.H - 1;
-    if (dy == 0) { x = xe; y = line; len = P.W; }
-    else if (dx == 0) { x = line; y = ye; len = P.H; }
-    else {
-        if (line < P.H) { x = xe; y = line; }
-        else { x = xe + dx * (line - P.H + 1); y = ye; }
-        len = min(dx > 0 ? P.W - x : x + 1, dy > 0 ? P.H - y : y + 1);
-    }
-    if (line >= P.nlines) len = 0;
-}
-
 }  // namespace
 
 // Runs warp `warp` of a pass over lines 2*warp and 2*warp+1, in any mode:
@@ -148,8 +134,8 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     const int la = 2 * warp;
     if (la >= P.nlines) return;                       // whole warp leaves together
     int xa, ya, lena, xb, yb, lenb;
-    line_geo(P, la, xa, ya, lena);
-    line_geo(P, la + 1, xb, yb, lenb);                // lenb = 0 if there is no second line
+    line_start(P, la, xa, ya, lena);
+    line_start(P, la + 1, xb, yb, lenb);              // lenb = 0 if there is no second line
     const int maxlen = max(lena, lenb), minlen = lenb ? min(lena, lenb) : lena;
     const int dx = P.dx, dy = P.dy, step = dy * P.W + dx;
     int pa = ya * P.W + xa, pb = yb * P.W + xb;
@@ -166,6 +152,9 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     long long goff = ((long long)(gl ? pb : pa) + (long long)gk * step) * D + go;
     const int glim = (gl ? lenb : lena) - gk;
     long long ooff = goff;                            // scratch output: same granules, plane P.sc
+    // even_only: only pixels with x and y both even are stored (a chunk is an
+    // even number of steps: a granule's parity is the same in every chunk)
+    const bool ost = !P.even_only || ((((gl ? xb : xa) + gk * dx) | ((gl ? yb : ya) + gk * dy)) & 1) == 0;
     long long soff[2];
     int slim[2];
 #pragma unroll
@@ -330,7 +319,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         }
         if (MODE == MODE_SCRATCH) {
             __syncwarp();                             // every lane's L bytes of the chunk are staged
-            if (ch * K < glim) *(uint4 *)(P.sc + ooff) = *(const uint4 *)(chunk + gb);
+            if (ost && ch * K < glim) *(uint4 *)(P.sc + ooff) = *(const uint4 *)(chunk + gb);
             ooff += adv;
         }
     }

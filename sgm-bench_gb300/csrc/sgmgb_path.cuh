@@ -45,6 +45,36 @@ namespace {
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr uint32_t kPadPk = 0x3FFF3FFFu;   // cost / L of lanes past the last disparity
 
+// Entry pixel (x, y) and length of line `line` of a pass (len = 0 past
+// P.nlines). Lines run along (dx, dy) from the image edge they enter by: rows,
+// columns, or diagonals indexed first by entry row, then by entry column.
+// P.even_only (multi-scale full scale; W and H even): only the lines that
+// cross a pixel with x and y both even are enumerated -- even rows, even
+// columns, and the diagonals whose x + y is even (every other diagonal in
+// each of the two entry edges).
+__device__ __forceinline__ void line_start(const LineParams &P, int line, int &x, int &y, int &len) {
+    const int dx = P.dx, dy = P.dy;
+    const int xe = dx > 0 ? 0 : P.W - 1, ye = dy > 0 ? 0 : P.H - 1;
+    int l = line;
+    if (P.even_only) {
+        if (dx == 0 || dy == 0) {
+            l = 2 * line;
+        } else {
+            const int n1 = (P.H - (xe & 1) + 1) >> 1;     // entry rows l with xe + l even
+            if (line < n1) l = (xe & 1) + 2 * line;
+            else l = P.H - 1 + (((xe + ye) & 1) ? 1 : 2) + 2 * (line - n1);   // entry column xe + dx*(l-H+1)
+        }
+    }
+    if (dy == 0) { x = xe; y = l; len = P.W; }
+    else if (dx == 0) { x = l; y = ye; len = P.H; }
+    else {
+        if (l < P.H) { x = xe; y = l; }
+        else { x = xe + dx * (l - P.H + 1); y = ye; }
+        len = min(dx > 0 ? P.W - x : x + 1, dy > 0 ? P.H - y : y + 1);
+    }
+    if (line >= P.nlines) len = 0;
+}
+
 __device__ __forceinline__ uint32_t vmin2(uint32_t a, uint32_t b) {
     uint32_t r;
     asm("min.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
@@ -280,17 +310,9 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
     const int dx = P.dx, dy = P.dy;
 
     // entry pixel and length of this group's line
-    const int xe = dx > 0 ? 0 : P.W - 1, ye = dy > 0 ? 0 : P.H - 1;
-    int x, y, len = 0;
-    if (dy == 0) { x = xe; y = line; }
-    else if (dx == 0) { x = line; y = ye; }
-    else if (line < P.H) { x = xe; y = line; }
-    else { x = xe + dx * (line - P.H + 1); y = ye; }
-    if (active) {
-        if (dy == 0) len = P.W;
-        else if (dx == 0) len = P.H;
-        else len = min(dx > 0 ? P.W - x : x + 1, dy > 0 ? P.H - y : y + 1);
-    }
+    int x, y, len;
+    line_start(P, line, x, y, len);
+    if (!active) len = 0;
     const int maxlen = __reduce_max_sync(kFull, (uint32_t)len);
     const int step = dy * P.W + dx;
     int p = y * P.W + x;
@@ -315,9 +337,17 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
     }
     // SCRATCH: the plane has the cost volume's layout, so the chunk's L bytes,
     // staged where its cost bytes were, go out by the same 16-byte granules.
+    // even_only: only the granules of pixels with x and y even (a chunk is an
+    // even number of steps, so a granule's parity is the same in every chunk).
     long long ooff[NGB];
+    bool ost[NGB];
 #pragma unroll
-    for (int j = 0; j < NGB; j++) ooff[j] = goff[j];
+    for (int j = 0; j < NGB; j++) {
+        ooff[j] = goff[j];
+        const int b = (lane + 32 * j) * 16, k = b / SBM, gg = min((b % SBM) / P.D, 31);
+        const int xg = __shfl_sync(kFull, x, (gg * LPL) & 31), yg = __shfl_sync(kFull, y, (gg * LPL) & 31);
+        ost[j] = !P.even_only || (((xg + k * dx) | (yg + k * dy)) & 1) == 0;
+    }
     long long soff[HAS_S ? 2 * NGB : 1];
     int slim[HAS_S ? 2 * NGB : 1];
     if (HAS_S) {
@@ -488,7 +518,7 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
                 __syncwarp();           // every lane's L bytes of the chunk are staged
 #pragma unroll
                 for (int j = 0; j < NGB; j++) {
-                    if (ch * K < glim[j])
+                    if (ost[j] && ch * K < glim[j])
                         *(uint4 *)(P.sc + ooff[j]) = *(const uint4 *)(chunk + (lane + 32 * j) * 16);
                     ooff[j] += adv;
                 }

@@ -153,7 +153,7 @@ cudaError_t run_final(const FrameSlot &s, const LineParams &base, int npaths, in
         LineParams q = base;
         q.dx = dirs[k][0]; q.dy = dirs[k][1]; q.sc = pl[k];
         q.p1 = ms ? ms_p1(q.dx, q.dy) : 20;
-        q.nlines = lines_for(q.W, q.H, q.dx, q.dy);
+        q.nlines = q.even_only ? lines_for_even(q.W, q.H, q.dx, q.dy) : lines_for(q.W, q.H, q.dx, q.dy);
         if ((e = launch_line(q, MODE_SCRATCH, sat, wpb, ss[k])) != cudaSuccess) return e;
         if ((e = mark(pass_name(q.dx, q.dy), 2 * ND)) != cudaSuccess) return e;
     }
@@ -168,9 +168,9 @@ cudaError_t run_final(const FrameSlot &s, const LineParams &base, int npaths, in
     q.sc = pl[0]; q.sc2 = pl[1]; q.sc3 = pl[2];
     for (int k = 0; k < 4; k++) q.xpl[k] = npaths == 8 ? pl[3 + k] : nullptr;
     q.p1 = ms ? ms_p1(0, 1) : 20;
-    q.nlines = lines_for(q.W, q.H, 0, 1);
     q.disp = disp;
     q.even_only = even_only;
+    q.nlines = even_only ? lines_for_even(q.W, q.H, 0, 1) : lines_for(q.W, q.H, 0, 1);
     q.key16 = (npaths == 4 && base.D <= 64) ? 1 : 0;   // S*64 + d < 2^16
     if ((e = launch_line(q, npaths == 8 ? MODE_FINAL7 : MODE_FINAL3, sat, wpb, st)) != cudaSuccess) return e;
     return mark("path_tb_final", npaths * ND + Nout);
@@ -203,7 +203,7 @@ cudaError_t run_planes(const FrameSlot &s, const LineParams &base, int npaths, i
         LineParams q = base;
         q.dx = dirs[k][0]; q.dy = dirs[k][1]; q.sc = pl[k];
         q.p1 = ms ? ms_p1(q.dx, q.dy) : 20;
-        q.nlines = lines_for(q.W, q.H, q.dx, q.dy);
+        q.nlines = q.even_only ? lines_for_even(q.W, q.H, q.dx, q.dy) : lines_for(q.W, q.H, q.dx, q.dy);
         sp.p[k] = pl[k];
         if ((e = launch_line(q, MODE_SCRATCH, sat, wpb, ss[k])) != cudaSuccess) return e;
         if ((e = mark(pass_name(q.dx, q.dy), 2 * ND)) != cudaSuccess) return e;
