@@ -210,7 +210,10 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         for (int j = 0; j < NR; j++) {
             const uint32_t lo = j == 0 ? up : L[j - 1];
             const uint32_t hi = j == NR - 1 ? dn : L[j + 1];
-            w[j] = vmin2(L[j], vmin2(lo, hi) + P1);
+            if (NR >= 4)   // measured: faster at D = 128, slower at D = 64
+                w[j] = j == 0 ? nbr_min(L[j], hi, lo, P1) : nbr_min(L[j], lo, hi, P1);
+            else
+                w[j] = vmin2(L[j], vmin2(lo, hi) + P1);
         }
         const uint32_t E = mn + P2;
         uint32_t tm = kFull;

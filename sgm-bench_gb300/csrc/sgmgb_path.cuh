@@ -80,6 +80,12 @@ __device__ __forceinline__ uint32_t vmin2(uint32_t a, uint32_t b) {
     asm("min.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
     return r;
 }
+// min(L, early + P1, late + P1) per half (the neighbour terms of the
+// recurrence) with two fused add-min operations; `late` (the operand that
+// comes from a shuffle) enters last. No half exceeds 0x7FFF, so nothing wraps.
+__device__ __forceinline__ uint32_t nbr_min(uint32_t L, uint32_t early, uint32_t late, uint32_t P1) {
+    return __viaddmin_u16x2(late, P1, __viaddmin_u16x2(early, P1, L));
+}
 // min of the two halves, replicated into both halves
 __device__ __forceinline__ uint32_t fold2(uint32_t v) { return vmin2(v, __byte_perm(v, v, 0x1032)); }
 __device__ __forceinline__ uint32_t pk2(uint32_t v) { return v | (v << 16); }
@@ -461,7 +467,10 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
         for (int j = 0; j < NR; j++) {
             const uint32_t lo = j == 0 ? lo0 : L[j - 1];
             const uint32_t hi = j == NR - 1 ? hiL : L[j + 1];
-            w[j] = vmin2(L[j], vmin2(lo, hi) + P1);
+            if (NR >= 2)   // measured: faster from DPL = 4 on, slower at DPL = 2
+                w[j] = j == 0 ? nbr_min(L[j], hi, lo, P1) : nbr_min(L[j], lo, hi, P1);
+            else
+                w[j] = vmin2(L[j], vmin2(lo, hi) + P1);
         }
         const uint32_t E = mn + P2;
         uint32_t tm = kFull;
