@@ -100,4 +100,13 @@ cudaError_t launch_half2(const uint8_t *im0, const uint8_t *im1, uint8_t *out0, 
     return cudaGetLastError();
 }
 
+cudaError_t prepare_frame_kernels() {
+    cudaError_t e = set_carveout(k_census2);
+    if (e == cudaSuccess) e = set_carveout(k_cost<false>);
+    if (e == cudaSuccess) e = set_carveout(k_cost<true>);
+    if (e == cudaSuccess) e = set_carveout(k_sobel2);
+    if (e == cudaSuccess) e = set_carveout(k_half2);
+    return e;
+}
+
 }  // namespace sgmgb

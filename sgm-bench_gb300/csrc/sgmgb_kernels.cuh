@@ -79,9 +79,21 @@ cudaError_t launch_half2(const uint8_t *im0, const uint8_t *im1, uint8_t *out0, 
 // multi-scale full-scale cost averaged with the half-scale volume C1.
 cudaError_t launch_cost(const uint64_t *cl, const uint64_t *cr, uint8_t *C, const uint8_t *C1,
                         int W, int H, int D, int invalid, cudaStream_t s);
-// Sets the path kernels' shared-memory limits; call once per device before
-// the first launch (and outside stream capture).
+// Sets the kernels' shared-memory limits and carve-out; call once per device
+// before the first launch (and outside stream capture). The census, cost,
+// prefilter and path kernels ask for the same carve-out (the largest
+// shared-memory share), so the side-by-side passes of a frame, and frames in
+// flight, can share an SM: kernels that need different L1/shared splits
+// cannot (measured: 4 frames in flight 0.305 -> 0.294 ms per frame). The sum
+// pass runs alone after the join and streams through L1: it keeps the
+// default (the largest shared share measured 90 -> 98 us at 1080p D=64).
 cudaError_t prepare_path_kernels();
+cudaError_t prepare_frame_kernels();   // census, cost, prefilters (sgmgb_kernels.cu)
+template <typename K>
+inline cudaError_t set_carveout(K *kernel) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared);
+}
 // One direction's path pass over the cost volume p.C (sgmgb_path.cu).
 // saturate: clamp L to 255 (multi-scale). warps_per_block in 1..4.
 cudaError_t launch_line(const LineParams &p, int mode, int saturate, int warps_per_block, cudaStream_t s);

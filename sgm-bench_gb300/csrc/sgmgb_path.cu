@@ -24,8 +24,10 @@ k_pair(const LineParams P) {
 // ---------------------------------------------------------------------------
 template <int NR, int MODE, int SAT, bool KEY16>
 static cudaError_t prep_pair() {
-    return cudaFuncSetAttribute(k_pair<NR, MODE, SAT, KEY16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                4 * PairSlot<NR, MODE>::RING);
+    cudaError_t e = cudaFuncSetAttribute(k_pair<NR, MODE, SAT, KEY16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         4 * PairSlot<NR, MODE>::RING);
+    if (e == cudaSuccess) e = set_carveout(k_pair<NR, MODE, SAT, KEY16>);
+    return e;
 }
 
 template <int NR, int SAT>
@@ -88,8 +90,10 @@ static cudaError_t launch_pair(const LineParams &p, int mode, int saturate, int 
 
 template <int DPL, int MODE, int SAT, bool KEY16>
 static cudaError_t prep_one() {
-    return cudaFuncSetAttribute(k_path<DPL, MODE, SAT, KEY16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                4 * Slot<DPL, MODE>::RING);
+    cudaError_t e = cudaFuncSetAttribute(k_path<DPL, MODE, SAT, KEY16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         4 * Slot<DPL, MODE>::RING);
+    if (e == cudaSuccess) e = set_carveout(k_path<DPL, MODE, SAT, KEY16>);
+    return e;
 }
 
 template <int DPL, int SAT, bool KEY16>
@@ -105,6 +109,7 @@ static cudaError_t prep_dpl() {
 
 cudaError_t prepare_path_kernels() {
     cudaError_t e;
+    if ((e = prepare_frame_kernels()) != cudaSuccess) return e;
     if ((e = prep_pair_modes<1, 0>()) != cudaSuccess) return e;
     if ((e = prep_pair_modes<2, 0>()) != cudaSuccess) return e;
     if ((e = prep_pair_modes<4, 0>()) != cudaSuccess) return e;
