@@ -462,6 +462,17 @@ static int cuda_fail(sgmgb_ctx *ctx, cudaError_t e, const char *what) {
     return set_err(ctx, SGMGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// A device-usable address of host memory that is page-locked or registered
+// with CUDA, or NULL for any other pointer (pageable host memory).
+static const uint8_t *host_view(const void *p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost && a.devicePointer ? (const uint8_t *)a.devicePointer : nullptr;
+}
+
 int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right, uint8_t *disp,
                     sgmgb_stage_times *t) {
     if (!ctx || !left || !right || !disp) return SGMGB_ERR_ARG;
@@ -472,17 +483,25 @@ int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right, u
     int ow = 0, oh = 0;
     sgmgb_out_size(&s.fd, &ow, &oh);
     const size_t outN = (size_t)ow * oh;
-    // copies in, the frame, the copy out: one stream, one wait at the end
-    // (copies of the two images on two streams measured slower)
+    // Page-locked (or registered) host buffers cross NVLink-C2C inside the
+    // kernels: the first kernels read the images from host memory and the sum
+    // pass of the latency schedule writes the map into it, so the transfers
+    // overlap the compute. Other host buffers go through the copy engines.
+    // (Measured slower: the two images on two streams; the images in two row
+    // bands with the census of the top band started early.) One stream, one
+    // wait at the end.
     cudaStream_t st = ctx->stream;
+    const PathShape shape = resolve_sched(ctx->shape, true);
+    const uint8_t *hl = host_view(left), *hr = host_view(right);
+    uint8_t *hd = shape.sched == SGMGB_SCHED_LATENCY ? (uint8_t *)host_view(disp) : nullptr;
     cudaEvent_t *ev = ctx->ev;   // 0 start, 3 inputs in, 1 census and cost done, 2 frame done, 4 map out
     cudaError_t e = cudaEventRecord(ev[0], st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s.left, left, N, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s.right, right, N, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !hl) e = cudaMemcpyAsync(s.left, left, N, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !hr) e = cudaMemcpyAsync(s.right, right, N, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
     if (e == cudaSuccess)
-        e = enqueue_frame(s, s.left, s.right, s.disp, st, resolve_sched(ctx->shape, true), ev[1], ev[2]);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(disp, s.disp, outN, cudaMemcpyDeviceToHost, st);
+        e = enqueue_frame(s, hl ? hl : s.left, hr ? hr : s.right, hd ? hd : s.disp, st, shape, ev[1], ev[2]);
+    if (e == cudaSuccess && !hd) e = cudaMemcpyAsync(disp, s.disp, outN, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[4], st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "frame (copies and pipeline)");

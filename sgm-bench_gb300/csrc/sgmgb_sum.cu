@@ -35,6 +35,7 @@ template <int NP, bool KEY16, bool SHFL, bool EVEN>
 __global__ void __launch_bounds__(256) k_sum(SumPlanes pl, uint8_t *__restrict__ disp, int W, int D, int tpp,
                                              int lt, int npb, int ks) {
     __shared__ uint32_t s_key[SHFL ? 1 : 256];
+    __shared__ uint8_t s_out[256];
     const int t = threadIdx.x;
     const int ow = EVEN ? W >> 1 : W;
     const int lp = SHFL ? t >> lt : t / tpp, g = t - lp * tpp;
@@ -79,7 +80,11 @@ __global__ void __launch_bounds__(256) k_sum(SumPlanes pl, uint8_t *__restrict__
         if (live && g == 0)
             for (int i = 1; i < tpp; i++) key = min(key, s_key[t + i]);
     }
-    if (live && g == 0) disp[(size_t)oy * ow + ox] = (uint8_t)(key & (KEY16 ? (1u << ks) - 1u : 0xFFu));
+    if (live && g == 0) s_out[lp] = (uint8_t)(key & (KEY16 ? (1u << ks) - 1u : 0xFFu));
+    __syncthreads();
+    // the block's npb outputs are consecutive bytes of one row: one coalesced
+    // store per warp (the map may be the caller's pinned host buffer)
+    if (t < npb && blockIdx.x * npb + t < ow) disp[(size_t)oy * ow + blockIdx.x * npb + t] = s_out[t];
 }
 
 template <int NP, bool KEY16, bool EVEN>

@@ -251,15 +251,22 @@ class Engine:
                                             ctypes.byref(n)))
         return [(out[k].name.decode(), out[k].ms, out[k].bytes) for k in range(n.value)]
 
-    def run_frame(self, left, right, times=False):
-        """Host arrays in, host disparity map out (the drop-in call)."""
+    def run_frame(self, left, right, times=False, out=None):
+        """Host arrays in, host disparity map out (the drop-in call). `out`: a
+        C-contiguous uint8 array of the output size to fill (e.g. pinned memory,
+        which the kernels write directly), else a new array."""
         left = np.ascontiguousarray(left, np.uint8)
         right = np.ascontiguousarray(right, np.uint8)
         H, W = left.shape
         if self.fd is None or (self.fd.W, self.fd.H) != (W, H):
             raise SgmError(ERR_STATE, "plan() this size first")
         ow, oh = out_size(W, H, self.fd.D, self.fd.paths, self.fd.variant)
-        disp = np.empty((oh, ow), np.uint8)
+        if out is None:
+            disp = np.empty((oh, ow), np.uint8)
+        else:
+            if out.dtype != np.uint8 or out.shape != (oh, ow) or not out.flags["C_CONTIGUOUS"]:
+                raise SgmError(ERR_ARG, "out must be a C-contiguous uint8 array of shape %r" % ((oh, ow),))
+            disp = out
         st = StageTimes()
         self._check(lib.sgmgb_run_frame(self.h, left.ctypes.data, right.ctypes.data, disp.ctypes.data,
                                         ctypes.byref(st)))
