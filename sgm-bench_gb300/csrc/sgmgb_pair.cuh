@@ -34,20 +34,26 @@ namespace sgmgb {
 
 namespace {
 
-template <int NR> struct PairRing {
-    static constexpr int K = 8 / NR;                               // steps per chunk (512 B per stream)
+// A chunk is G 16-byte granules per lane of each input stream: 512 G bytes,
+// K = 8 G / NR steps. The scratch passes (one input stream) take chunks of
+// 1 KB: half the per-chunk waits, copies and stores per step; the other modes
+// keep 512 bytes, which bounds the registers their chunk inputs take.
+template <int NR, int MODE> struct PairRing {
+    static constexpr int G = MODE == MODE_SCRATCH ? 2 : 1;         // granules per lane per stream
+    static constexpr int CB = 512 * G;                             // bytes of one stream per chunk
+    static constexpr int K = 8 * G / NR;                           // steps per chunk
     static constexpr int NCH = NR == 1 ? 4 : (NR == 2 ? 6 : 8);    // ring depth in chunks
     static constexpr int SB = 64 * NR;                             // bytes of one stream per step: [A | B]
 };
-// Streams of a chunk slot, in 512-byte units: the cost bytes, the planes the
-// pass reads (one: sc; three for FINAL3), and the partial sum S (uint16, two
-// units) for ACCUM and FINAL.
+// Streams of a chunk slot, in units of CB bytes: the cost bytes, the planes
+// the pass reads (one: sc; three for FINAL3), and the partial sum S (uint16,
+// two units) for ACCUM and FINAL.
 template <int NR, int MODE> struct PairSlot {
     static constexpr int NPL = MODE == MODE_SCRATCH ? 0 : (MODE == MODE_FINAL3 ? 3 : 1);
     static constexpr bool HAS_S = MODE == MODE_ACCUM || MODE == MODE_FINAL;
     static constexpr int U = 1 + NPL + (HAS_S ? 2 : 0);
-    static constexpr int BYTES = 512 * U;
-    static constexpr int RING = PairRing<NR>::NCH * BYTES;
+    static constexpr int BYTES = PairRing<NR, MODE>::CB * U;
+    static constexpr int RING = PairRing<NR, MODE>::NCH * BYTES;
 };
 
 // NR bytes from shared memory, zero-extended into a word (NR = 1, 2) or a word (NR = 4).
@@ -124,7 +130,8 @@ __device__ __forceinline__ void st_run(uint8_t *p, uint32_t v) {
 // bytes of shared memory (16-byte aligned). All 32 lanes must call it.
 template <int NR, int MODE, int SAT, bool KEY16>
 __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t *ring) {
-    constexpr int K = PairRing<NR>::K, NCH = PairRing<NR>::NCH, SB = PairRing<NR>::SB;
+    using RG = PairRing<NR, MODE>;
+    constexpr int K = RG::K, NCH = RG::NCH, SB = RG::SB, G = RG::G, CB = RG::CB;
     constexpr int NPL = PairSlot<NR, MODE>::NPL;
     constexpr bool HAS_S = PairSlot<NR, MODE>::HAS_S;
     constexpr int SLOT = PairSlot<NR, MODE>::BYTES;
@@ -143,22 +150,29 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     const uint32_t mlo = (NR == 4 && lane == 0) ? 0x3FFF3FFFu : 0u;    // d = -1 does not exist
     const uint32_t mhi = (NR == 4 && lane == 31) ? 0x3FFF3FFFu : 0u;   // d = D does not exist
 
-    // this lane's 16-byte granules of every chunk. Byte streams (cost, planes):
-    // step k = b / SB, line b % SB / D, byte b % D. The sum S (2 units): two
-    // granules, step b / (2 SB), line b % (2 SB) / (2D), byte b % (2D).
+    // this lane's 16-byte granules u = lane + 32 h (h < G) of every chunk.
+    // Byte streams (cost, planes): byte b = 16 u is step b / SB, line
+    // b % SB / D, byte b % D. The sum S (2 units): granules u < 64 G, step
+    // b / (2 SB), line b % (2 SB) / (2D), byte b % (2D).
     const uint32_t ring_s = (uint32_t)__cvta_generic_to_shared(ring);
-    const int gb = lane * 16, gk = gb / SB, gr = gb % SB, gl = gr / D, go = gr - gl * D;
     const long long adv = (long long)K * step * D;
-    long long goff = ((long long)(gl ? pb : pa) + (long long)gk * step) * D + go;
-    const int glim = (gl ? lenb : lena) - gk;
-    long long ooff = goff;                            // scratch output: same granules, plane P.sc
-    // even_only: only pixels with x and y both even are stored (a chunk is an
-    // even number of steps: a granule's parity is the same in every chunk)
-    const bool ost = !P.even_only || ((((gl ? xb : xa) + gk * dx) | ((gl ? yb : ya) + gk * dy)) & 1) == 0;
-    long long soff[2];
-    int slim[2];
+    long long goff[G], ooff[G];
+    int glim[G];
+    bool ost[G];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < G; h++) {
+        const int gb = (lane + 32 * h) * 16, gk = gb / SB, gr = gb % SB, gl = gr / D, go = gr - gl * D;
+        goff[h] = ((long long)(gl ? pb : pa) + (long long)gk * step) * D + go;
+        glim[h] = (gl ? lenb : lena) - gk;
+        ooff[h] = goff[h];                            // scratch output: same granules, plane P.sc
+        // even_only: only pixels with x and y both even are stored (a chunk is
+        // an even number of steps: a granule's parity is the same in every chunk)
+        ost[h] = !P.even_only || ((((gl ? xb : xa) + gk * dx) | ((gl ? yb : ya) + gk * dy)) & 1) == 0;
+    }
+    long long soff[2 * G];
+    int slim[2 * G];
+#pragma unroll
+    for (int h = 0; h < 2 * G; h++) {
         const int b = (lane + 32 * h) * 16, k = b / (2 * SB), r = b % (2 * SB), l = r / (2 * D), o = r - l * 2 * D;
         soff[h] = ((long long)(l ? pb : pa) + (long long)k * step) * 2 * D + o;
         slim[h] = HAS_S ? (l ? lenb : lena) - k : 0;
@@ -169,16 +183,20 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     if (NPL == 3) { src[2] = P.sc2; src[3] = P.sc3; }
     auto issue = [&](int c) {
         const uint32_t dst = ring_s + (uint32_t)((c % NCH) * SLOT);
-        if (c * K < glim) {
 #pragma unroll
-            for (int q = 0; q <= NPL; q++) cp_async16(dst + (uint32_t)(q * 512 + gb), src[q] + goff);
+        for (int h = 0; h < G; h++) {
+            if (c * K < glim[h]) {
+#pragma unroll
+                for (int q = 0; q <= NPL; q++)
+                    cp_async16(dst + (uint32_t)(q * CB + (lane + 32 * h) * 16), src[q] + goff[h]);
+            }
+            goff[h] += adv;
         }
-        goff += adv;
         if (HAS_S) {
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
+            for (int h = 0; h < 2 * G; h++) {
                 if (c * K < slim[h])
-                    cp_async16(dst + (uint32_t)((1 + NPL) * 512 + (lane + 32 * h) * 16), (const uint8_t *)P.S + soff[h]);
+                    cp_async16(dst + (uint32_t)((1 + NPL) * CB + (lane + 32 * h) * 16), (const uint8_t *)P.S + soff[h]);
                 soff[h] += 2 * adv;
             }
         }
@@ -300,9 +318,9 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             pair_unpack<NR>(ld_run<NR>(r), ld_run<NR>(r + D), c[k]);
 #pragma unroll
             for (int q = 0; q < NPL; q++)
-                pair_unpack<NR>(ld_run<NR>(r + (q + 1) * 512), ld_run<NR>(r + (q + 1) * 512 + D), pl[k][q]);
+                pair_unpack<NR>(ld_run<NR>(r + (q + 1) * CB), ld_run<NR>(r + (q + 1) * CB + D), pl[k][q]);
             if (HAS_S) {
-                const uint8_t *sr = chunk + (1 + NPL) * 512 + k * 2 * SB + lane * 2 * NR;
+                const uint8_t *sr = chunk + (1 + NPL) * CB + k * 2 * SB + lane * 2 * NR;
                 uint32_t sa[NR > 1 ? NR / 2 : 1], sb[NR > 1 ? NR / 2 : 1];
                 if (NR == 1) { sa[0] = *(const uint16_t *)sr; sb[0] = *(const uint16_t *)(sr + 2 * D); }
                 else if (NR == 2) { sa[0] = *(const uint32_t *)sr; sb[0] = *(const uint32_t *)(sr + 2 * D); }
@@ -322,8 +340,12 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         }
         if (MODE == MODE_SCRATCH) {
             __syncwarp();                             // every lane's L bytes of the chunk are staged
-            if (ost && ch * K < glim) *(uint4 *)(P.sc + ooff) = *(const uint4 *)(chunk + gb);
-            ooff += adv;
+#pragma unroll
+            for (int h = 0; h < G; h++) {
+                if (ost[h] && ch * K < glim[h])
+                    *(uint4 *)(P.sc + ooff[h]) = *(const uint4 *)(chunk + (lane + 32 * h) * 16);
+                ooff[h] += adv;
+            }
         }
     }
     cp_async_wait<0>();                               // no copy outlives the kernel
