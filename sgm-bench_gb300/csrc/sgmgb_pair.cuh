@@ -24,8 +24,8 @@
 // pixel of a line starts from L_prev = 0, min_prev = 0, which yields L = C.
 //
 // Memory: the per-warp shared-memory ring of sgmgb_path.cuh, a step being the
-// two lines' D-byte rows [A | B] of each input stream; a chunk is 512 bytes of
-// a stream (one 16-byte cp.async granule per lane). The scratch output is
+// two lines' D-byte rows [A | B] of each input stream; a chunk is G 16-byte
+// cp.async granules per lane of a stream (PairRing). The scratch output is
 // staged in the consumed cost rows and leaves by the same granules.
 #pragma once
 #include "sgmgb_path.cuh"
@@ -36,10 +36,12 @@ namespace {
 
 // A chunk is G 16-byte granules per lane of each input stream: 512 G bytes,
 // K = 8 G / NR steps. The scratch passes (one input stream) take chunks of
-// 1 KB: half the per-chunk waits, copies and stores per step; the other modes
-// keep 512 bytes, which bounds the registers their chunk inputs take.
+// 1 KB (2 KB at D = 128): fewer per-chunk waits, copies and stores per step
+// (measured at D = 64: 512 B 125 us, 1 KB 94 us, 2 KB 98 us per row pass; at
+// D = 128: 1 KB 167 us, 2 KB 143 us). The other modes keep 512 bytes, which
+// bounds the registers their chunk inputs take.
 template <int NR, int MODE> struct PairRing {
-    static constexpr int G = MODE == MODE_SCRATCH ? 2 : 1;         // granules per lane per stream
+    static constexpr int G = MODE == MODE_SCRATCH ? (NR == 4 ? 4 : 2) : 1;   // granules per lane per stream
     static constexpr int CB = 512 * G;                             // bytes of one stream per chunk
     static constexpr int K = 8 * G / NR;                           // steps per chunk
     static constexpr int NCH = NR == 1 ? 4 : (NR == 2 ? 6 : 8);    // ring depth in chunks

@@ -132,19 +132,22 @@ template <int MODE> struct Planes {   // scratch planes a pass reads
 // plane: D bytes per line) takes SBM = 32*DPL bytes of the ring whatever the
 // group shape, so lane l always reads its DPL bytes at l*DPL; the partial sum
 // S takes two such units. NGB: 16-byte copies per lane per byte stream per chunk.
-template <int DPL> struct Ring {
-    static constexpr int K = 16 / DPL;             // steps per chunk: 512 ring bytes per byte stream
+template <int DPL, int MODE> struct Ring {
+    // steps per chunk: 1 KB of ring per byte stream for the scratch passes
+    // (one stream: fewer per-chunk waits, copies and stores per step), 512 B
+    // for the modes with more streams (registers for the chunk's inputs)
+    static constexpr int K = (MODE == MODE_SCRATCH ? 32 : 16) / DPL;
     static constexpr int NCH = DPL == 2 ? 4 : (DPL == 4 ? 6 : 8);   // ring depth in chunks (NCH-1 in flight)
     static constexpr int SBM = 32 * DPL;
-    static constexpr int NGB = K * SBM / 512;      // = 1
+    static constexpr int NGB = K * SBM / 512;      // 2 (scratch) or 1
 };
 template <int DPL, int MODE> struct Slot {
     static constexpr bool HAS_S = MODE == MODE_ACCUM || MODE == MODE_FINAL;
     static constexpr int U = 1 + Planes<MODE>::N + (HAS_S ? 2 : 0);   // byte-stream units per step
-    static constexpr int BYTES = Ring<DPL>::K * Ring<DPL>::SBM * U;  // one chunk of a warp
+    static constexpr int BYTES = Ring<DPL, MODE>::K * Ring<DPL, MODE>::SBM * U;  // one chunk of a warp
     // ring depth: a chunk of eight streams (FINAL7) already carries 4 KB, so
     // two chunks in flight keep as many bytes moving as deeper rings of one
-    static constexpr int NCH = U >= 8 ? 3 : Ring<DPL>::NCH;
+    static constexpr int NCH = U >= 8 ? 3 : Ring<DPL, MODE>::NCH;
     static constexpr int RING = NCH * BYTES;                          // a warp's whole ring
 };
 
@@ -171,7 +174,7 @@ __device__ __forceinline__ void load_bytes(const uint8_t *src, uint32_t *w) {
 // Reads step k's inputs of this lane from the ring chunk at `chunk`.
 template <int DPL, int MODE>
 __device__ __forceinline__ void ring_read(const uint8_t *chunk, int lane, int k, StepIn<DPL, MODE> &s) {
-    constexpr int K = Ring<DPL>::K, SBM = Ring<DPL>::SBM, SCW = StepIn<DPL, MODE>::SCW;
+    constexpr int K = Ring<DPL, MODE>::K, SBM = Ring<DPL, MODE>::SBM, SCW = StepIn<DPL, MODE>::SCW;
     const uint8_t *b = chunk + k * SBM + lane * DPL;
     load_bytes<DPL>(b, s.cw);
 #pragma unroll
@@ -293,7 +296,8 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
 template <int DPL, int MODE, int SAT, bool KEY16>
 __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t *ring) {
     constexpr int NR = DPL / 2;
-    constexpr int K = Ring<DPL>::K, SBM = Ring<DPL>::SBM, NGB = Ring<DPL>::NGB, NCH = Slot<DPL, MODE>::NCH;
+    constexpr int K = Ring<DPL, MODE>::K, SBM = Ring<DPL, MODE>::SBM, NGB = Ring<DPL, MODE>::NGB,
+                  NCH = Slot<DPL, MODE>::NCH;
     constexpr int NPL = Planes<MODE>::N;
     constexpr bool HAS_S = Slot<DPL, MODE>::HAS_S;
     constexpr int SLOT = Slot<DPL, MODE>::BYTES;
