@@ -115,7 +115,10 @@ int  sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule);
 
 /* ---- single frame ---- */
 /* Host buffers in and out, synchronous: the drop-in call. left/right are
- * W*H bytes, row-major; disp receives the output map (sgmgb_out_size). */
+ * W*H bytes, row-major; disp receives the output map (sgmgb_out_size).
+ * Page-locked (or CUDA-registered) buffers are read and written across
+ * NVLink-C2C by the kernels themselves; other host memory goes through the
+ * copy engines. Runs the latency schedule under SGMGB_SCHED_AUTO. */
 int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right,
                     uint8_t *disp, sgmgb_stage_times *t);
 /* Device buffers, enqueued on `stream` (a cudaStream_t, NULL = the context's
