@@ -296,6 +296,39 @@ def cpu_baseline_sample(seconds, left, right, gpu_maps, ms_checks=()):
                       % (n, W, H, D, PATHS, el)}, exact, ms_exact
 
 
+def sweep_section(sgmgb, torch, np, warmup=10, frames=60):
+    """The reference's disparity-range x resolution grid (scripts/sweep.sh:20-56):
+    D in {32, 64, 128} x {1920x1080, 1280x720, 960x540, 640x480}, 4 paths, plus
+    D = 256 at 1920x1080, timed like the reference's harness cell (-w 10 -n 60):
+    the median wall time of the drop-in call on pinned host buffers, copies in
+    and out included. The golden of every cell, with the reference's
+    discrimination gate, is checked in tests/test_gpu_sweep.py; here the scene
+    is this package's generator at the cell's D."""
+    cells = [(D, W, H) for D in (32, 64, 128) for (W, H) in ((1920, 1080), (1280, 720), (960, 540), (640, 480))]
+    cells.append((256, 1920, 1080))
+    eng = sgmgb.Engine(0)
+    out = []
+    for D, W, H in cells:
+        l, r, _ = sgmgb.synth_pair(W, H, min(D, 200), 1)
+        hl = torch.from_numpy(l).pin_memory().numpy()
+        hr = torch.from_numpy(r).pin_memory().numpy()
+        ho = torch.empty((H, W), dtype=torch.uint8).pin_memory().numpy()
+        eng.plan(W, H, D, 4)
+        for _ in range(warmup):
+            eng.run_frame(hl, hr, out=ho)
+        lat = []
+        for _ in range(frames):
+            t0 = time.perf_counter()
+            eng.run_frame(hl, hr, out=ho)
+            lat.append(time.perf_counter() - t0)
+        med = statistics.median(lat) * 1e3
+        out.append({"D": D, "W": W, "H": H, "median_ms": round(med, 4), "fps": round(1e3 / med, 1),
+                    "mde_per_s": round(W * H * D / med / 1e3, 1)})
+    eng.close()
+    return {"cells": out, "paths": 4, "timing": "median of %d drop-in calls after %d warm-up, pinned host "
+                                                "buffers" % (frames, warmup)}
+
+
 def multiscale_section(sgmgb, torch, np, steps=60, inflight=4):
     """Configurations B and C: the multi-scale 8-path variant at 1920x800 and
     1920x1080 (output (W/2)x(H/2)), frames in flight as in the main line;
@@ -334,12 +367,18 @@ def multiscale_section(sgmgb, torch, np, steps=60, inflight=4):
         e1.record(s0)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
-        # one frame at a time, host buffers (the drop-in call)
-        engs[0].run_frame(pairs[0][0], pairs[0][1])
-        t0 = time.perf_counter()
-        for _ in range(10):
-            engs[0].run_frame(pairs[0][0], pairs[0][1])
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / 10
+        # one frame at a time, pinned host buffers (the drop-in call)
+        hl = torch.from_numpy(pairs[0][0]).pin_memory().numpy()
+        hr = torch.from_numpy(pairs[0][1]).pin_memory().numpy()
+        ho = torch.empty((Hm // 2, Wm // 2), dtype=torch.uint8).pin_memory().numpy()
+        for _ in range(3):
+            engs[0].run_frame(hl, hr, out=ho)
+        lat = []
+        for _ in range(20):
+            t0 = time.perf_counter()
+            engs[0].run_frame(hl, hr, out=ho)
+            lat.append(time.perf_counter() - t0)
+        e2e_ms = statistics.median(lat) * 1e3
         work = ((Wm // 2) * (Hm // 2) + Wm * Hm) * 64
         out[name] = {"W": Wm, "H": Hm, "out": [Wm // 2, Hm // 2], "ms_per_frame": ms, "fps": 1e3 / ms,
                      "mde_per_s_work": work / (ms / 1e3) / 1e6, "frames_in_flight": inflight,
@@ -566,6 +605,8 @@ def run_gb300(args):
         args.cpu_seconds, pairs[0][0], pairs[0][1], maps0, ms_checks)
     if ms_exact is not None:
         line["multiscale"]["bit_exact_vs_oracle"] = ms_exact
+    if not args.no_sweep:
+        line["d_sweep"] = sweep_section(sgmgb, torch, np)
     if not args.no_batch:
         line["batched"] = batched_section(sgmgb.Engine, sgmgb, torch, np)
     if not args.no_serve:
@@ -590,6 +631,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form section")
     ap.add_argument("--no-multiscale", action="store_true", help="skip the configurations B/C section")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-form section")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the D x resolution grid")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
