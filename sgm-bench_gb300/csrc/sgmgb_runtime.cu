@@ -484,15 +484,17 @@ int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right, u
     sgmgb_out_size(&s.fd, &ow, &oh);
     const size_t outN = (size_t)ow * oh;
     // Page-locked (or registered) host buffers cross NVLink-C2C inside the
-    // kernels: the first kernels read the images from host memory and the sum
-    // pass of the latency schedule writes the map into it, so the transfers
-    // overlap the compute. Other host buffers go through the copy engines.
-    // (Measured slower: the two images on two streams; the images in two row
-    // bands with the census of the top band started early.) One stream, one
-    // wait at the end.
+    // kernels: a plain frame's census reads the images from host memory (its
+    // 32-row tiles stage them with 16-byte loads) and the sum pass of the
+    // latency schedule writes the map into it, so the transfers overlap the
+    // compute. Other host buffers, and the multi-scale images (read byte by
+    // byte by its prefilters), go through the copy engines. (Measured slower:
+    // the two images on two streams; the images in two row bands with the
+    // census of the top band started early.) One stream, one wait at the end.
     cudaStream_t st = ctx->stream;
     const PathShape shape = resolve_sched(ctx->shape, true);
-    const uint8_t *hl = host_view(left), *hr = host_view(right);
+    const bool plain = s.fd.variant == SGMGB_PLAIN;
+    const uint8_t *hl = plain ? host_view(left) : nullptr, *hr = plain ? host_view(right) : nullptr;
     uint8_t *hd = shape.sched == SGMGB_SCHED_LATENCY ? (uint8_t *)host_view(disp) : nullptr;
     cudaEvent_t *ev = ctx->ev;   // 0 start, 3 inputs in, 1 census and cost done, 2 frame done, 4 map out
     cudaError_t e = cudaEventRecord(ev[0], st);

@@ -24,8 +24,10 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? l
 // descriptor. A tile is CEN_PX x CEN_ROWS pixels plus its 4/3-pixel halo,
 // staged in shared memory.
 // ---------------------------------------------------------------------------
-constexpr int CEN_PX = 128, CEN_ROWS = 8, CEN_TW = CEN_PX + 8, CEN_TH = CEN_ROWS + 6;
-constexpr int CEN_SMEM = CEN_TW * CEN_TH;            // bytes, 16-byte aligned by the caller
+constexpr int CEN_PX = 128, CEN_ROWS = 8, CEN_TW = CEN_PX + 8;
+// shared memory of a tile of R rows, 16-byte aligned by the caller
+template <int R> __host__ __device__ constexpr int cen_smem() { return CEN_TW * (R + 6); }
+constexpr int CEN_SMEM = cen_smem<CEN_ROWS>();
 
 __device__ __forceinline__ uint32_t bytes_lt(uint32_t n, uint32_t c, uint32_t c7) {
     // per byte: n < c, in the byte's top bit (the other bits are garbage)
@@ -42,12 +44,16 @@ __device__ __forceinline__ uint32_t window4(uint32_t w0, uint32_t w1, uint32_t w
     return s < 4 ? __byte_perm(w0, w1, sel) : __byte_perm(w1, w2, sel);
 }
 
-// Census of the tile at (x0, y0) of one W x H image into out (W*H uint64).
-// nthreads: a multiple of 32; tid in [0, nthreads). The image is read through
-// the read-only path: it is an input, never written during the launch.
+// Census of the CEN_PX x R tile at (x0, y0) of one W x H image into out
+// (W*H uint64). nthreads: a multiple of 32; tid in [0, nthreads). The image
+// is read through the read-only path: it is an input, never written during
+// the launch. Taller tiles read fewer halo rows per pixel (the 6 rows shared
+// with the tiles above and below): (R + 6) / R.
+template <int R = CEN_ROWS>
 __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint64_t *__restrict__ out,
                                             int W, int H, int x0, int y0, uint8_t *smem, int tid,
                                             int nthreads) {
+    constexpr int CEN_TH = R + 6, CEN_SMEM = cen_smem<R>();
     uint32_t *tile = (uint32_t *)smem;                // [CEN_TH][CEN_TW / 4]
     constexpr int RW = CEN_TW / 4;                    // words per tile row
     if ((W & 15) == 0 && ((uintptr_t)im & 15) == 0 && x0 >= 16 && x0 + CEN_PX + 16 <= W) {
@@ -73,7 +79,7 @@ __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint
         }
     }
     __syncthreads();
-    for (int job = tid; job < 32 * CEN_ROWS; job += nthreads) {
+    for (int job = tid; job < 32 * R; job += nthreads) {
         const int tx = job & 31, ty = job >> 5;
         const int x = x0 + 4 * tx, y = y0 + ty;
         if (x >= W || y >= H) continue;
