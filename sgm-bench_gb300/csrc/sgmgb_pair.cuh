@@ -39,9 +39,9 @@ namespace {
 // 1 KB (2 KB at D = 128): fewer per-chunk waits, copies and stores per step
 // (measured at D = 64: 512 B 125 us, 1 KB 94 us, 2 KB 98 us per row pass; at
 // D = 128: 1 KB 167 us, 2 KB 143 us). The other modes keep 512 bytes, which
-// bounds the registers their chunk inputs take (1 KB chunks made the T->B
-// final pass 168 -> 154 us alone but, at 96 registers, four frames in flight
-// 0.281 -> 0.299 ms per frame).
+// bounds their shared memory: 1 KB chunks made the T->B final pass 166 ->
+// 152 us alone, but its ring (four streams) then takes 96 KB per 4-warp block
+// and four frames in flight went 0.280 -> 0.292 ms per frame.
 template <int NR, int MODE> struct PairRing {
     static constexpr int G = MODE == MODE_SCRATCH ? (NR == 4 ? 4 : 2) : 1;   // granules per lane per stream
     static constexpr int CB = 512 * G;                             // bytes of one stream per chunk
@@ -221,7 +221,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     const int hw = P.W >> 1;
 
     // one step of both lines; `row`: this step's cost row in the chunk
-    auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&pl)[3][NR], const uint32_t (&sv)[NR], uint8_t *row,
+    auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&ps)[NR], const uint32_t (&sv)[NR], uint8_t *row,
                          int i, auto full_t) {
         constexpr bool FULL = decltype(full_t)::value;
         pa += step; pb += step; xa += dx; ya += dy; xb += dx; yb += dy;
@@ -259,8 +259,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         uint32_t tot[NR];                             // this pass's L plus what the pass reads, per half <= 8*255
 #pragma unroll
         for (int j = 0; j < NR; j++) {
-            tot[j] = L[j] + pl[0][j];
-            if (MODE == MODE_FINAL3) tot[j] += pl[1][j] + pl[2][j];
+            tot[j] = L[j] + ps[j];
             if (HAS_S) tot[j] += sv[j];
         }
         if (MODE == MODE_STORE || MODE == MODE_ACCUM) {
@@ -315,14 +314,21 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         __syncwarp();                                 // ... and every lane's; slot ch-1 is free
         issue(ch + NCH - 1);
         uint8_t *chunk = ring + (ch % NCH) * SLOT;
-        uint32_t c[K][NR], pl[K][3][NR], sv[K][NR];
+        // the chunk's inputs, read before its steps run: costs, the sum of the
+        // planes the pass reads (off the recurrence: it only enters the total),
+        // and the partial sum S
+        uint32_t c[K][NR], ps[K][NR], sv[K][NR];
 #pragma unroll
-        for (int k = 0; k < K; k++) {                 // the chunk's inputs, read before its steps run
+        for (int k = 0; k < K; k++) {
             const uint8_t *r = chunk + k * SB + lane * NR;
             pair_unpack<NR>(ld_run<NR>(r), ld_run<NR>(r + D), c[k]);
 #pragma unroll
-            for (int q = 0; q < NPL; q++)
-                pair_unpack<NR>(ld_run<NR>(r + (q + 1) * CB), ld_run<NR>(r + (q + 1) * CB + D), pl[k][q]);
+            for (int q = 0; q < NPL; q++) {
+                uint32_t pq[NR];
+                pair_unpack<NR>(ld_run<NR>(r + (q + 1) * CB), ld_run<NR>(r + (q + 1) * CB + D), pq);
+#pragma unroll
+                for (int j = 0; j < NR; j++) ps[k][j] = q == 0 ? pq[j] : ps[k][j] + pq[j];
+            }
             if (HAS_S) {
                 const uint8_t *sr = chunk + (1 + NPL) * CB + k * 2 * SB + lane * 2 * NR;
                 uint32_t sa[NR > 1 ? NR / 2 : 1], sb[NR > 1 ? NR / 2 : 1];
@@ -337,10 +343,10 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         }
         if ((ch + 1) * K <= minlen) {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(c[k], pl[k], sv[k], chunk + k * SB, ch * K + k, std::true_type{});
+            for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, std::true_type{});
         } else {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(c[k], pl[k], sv[k], chunk + k * SB, ch * K + k, std::false_type{});
+            for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, std::false_type{});
         }
         if (MODE == MODE_SCRATCH) {
             __syncwarp();                             // every lane's L bytes of the chunk are staged
