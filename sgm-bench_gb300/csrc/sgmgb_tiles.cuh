@@ -137,7 +137,7 @@ __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint
 // conflicts), and each pixel's 32 bytes of the warp are one sector in the
 // store. The population counts (2 POPC per cost) are the bound.
 // ---------------------------------------------------------------------------
-constexpr int COST_PX = 64;                           // 8 blocks of 8 pixels, or 4 of 16
+constexpr int COST_PX = 128;                          // 16 blocks of 8 pixels, or 8 of 16
 constexpr int COST_SMEM = (COST_PX + COST_PX + 256) * 8;   // bytes, 16-byte aligned by the caller
 
 // LD_CG: read the descriptors through L2 only (the batch kernel, where other
@@ -165,7 +165,9 @@ template <bool DG4, bool MS, bool EDGE, bool TAIL>
 __device__ __forceinline__ void cost_tasks(const uint64_t *sl, const uint64_t *sr, uint8_t *__restrict__ row,
                                            const uint8_t *__restrict__ C1, int W, int D, int invalid, int y,
                                            int x0, int tid, int nthreads) {
-    constexpr int DG = DG4 ? 4 : 2, PXW = 32 / DG, LNXB = DG4 ? 3 : 2;   // LNXB = log2(COST_PX / PXW)
+    constexpr int DG = DG4 ? 4 : 2, PXW = 32 / DG;
+    constexpr int LNXB = COST_PX / PXW == 16 ? 4 : (COST_PX / PXW == 8 ? 3 : 2);   // log2(COST_PX / PXW)
+    static_assert((1 << LNXB) * PXW == COST_PX, "a tile is a power-of-two number of pixel blocks");
     const int lane = tid & 31;
     const int pxl = lane / DG, dgl = lane & (DG - 1);
     const int ntask = ((D >> 3) / DG) << LNXB;
