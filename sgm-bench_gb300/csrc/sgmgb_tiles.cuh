@@ -44,6 +44,56 @@ __device__ __forceinline__ uint32_t window4(uint32_t w0, uint32_t w1, uint32_t w
     return s < 4 ? __byte_perm(w0, w1, sel) : __byte_perm(w1, w2, sel);
 }
 
+// The census jobs of a staged CEN_PX x R tile at (x0, y0): word `OFF + w` of
+// staged row r holds image bytes x0 - 4 + 4w .. x0 - 1 + 4w of image row
+// y0 - 3 + r (clamped), RW words per row. A job makes 4 horizontally adjacent
+// pixels. No barrier inside: the caller synchronises around it.
+template <int R>
+__device__ __forceinline__ void census_jobs(const uint32_t *tile, int RW, int OFF, uint64_t *__restrict__ out,
+                                            int W, int H, int x0, int y0, int tid, int nthreads) {
+    for (int job = tid; job < 32 * R; job += nthreads) {
+        const int tx = job & 31, ty = job >> 5;
+        const int x = x0 + 4 * tx, y = y0 + ty;
+        if (x >= W || y >= H) continue;
+        const uint32_t c = tile[(ty + 3) * RW + OFF + tx + 1], c7 = c & 0x7F7F7F7Fu;
+        uint32_t A[8];
+        uint32_t acc = 0;
+        int n = 0;
+#pragma unroll
+        for (int dy = -3; dy <= 3; dy++) {
+            const uint32_t *r = tile + (ty + 3 + dy) * RW + OFF + tx;
+            const uint32_t w0 = r[0], w1 = r[1], w2 = r[2];
+#pragma unroll
+            for (int dx = -4; dx <= 4; dx++) {
+                if (dx == 0 && dy == 0) continue;
+                acc = (acc >> 1) | (bytes_lt(window4(w0, w1, w2, 4 + dx), c, c7) & 0x80808080u);
+                if ((++n & 7) == 0) { A[(n >> 3) - 1] = acc; acc = 0; }
+            }
+        }
+        A[7] = acc >> 2;                              // bits 56..61: six compares, aligned to bit 0
+        uint64_t d[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t sel = i | ((i + 4) << 4);
+            const uint32_t lo = __byte_perm(__byte_perm(A[0], A[1], sel), __byte_perm(A[2], A[3], sel), 0x5410);
+            const uint32_t hi = __byte_perm(__byte_perm(A[4], A[5], sel), __byte_perm(A[6], A[7], sel), 0x5410);
+            d[i] = ((uint64_t)hi << 32) | lo;
+        }
+        uint64_t *o = out + (size_t)y * W + x;
+        if (x + 3 < W) {
+            if ((((size_t)y * W + x) & 1) == 0) {
+                ((ulonglong2 *)o)[0] = make_ulonglong2(d[0], d[1]);
+                ((ulonglong2 *)o)[1] = make_ulonglong2(d[2], d[3]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; i++) o[i] = d[i];
+            }
+        } else {
+            for (int i = 0; i < 4 && x + i < W; i++) o[i] = d[i];
+        }
+    }
+}
+
 // Census of the CEN_PX x R tile at (x0, y0) of one W x H image into out
 // (W*H uint64). nthreads: a multiple of 32; tid in [0, nthreads). The image
 // is read through the read-only path: it is an input, never written during
@@ -79,47 +129,7 @@ __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint
         }
     }
     __syncthreads();
-    for (int job = tid; job < 32 * R; job += nthreads) {
-        const int tx = job & 31, ty = job >> 5;
-        const int x = x0 + 4 * tx, y = y0 + ty;
-        if (x >= W || y >= H) continue;
-        const uint32_t c = tile[(ty + 3) * RW + tx + 1], c7 = c & 0x7F7F7F7Fu;
-        uint32_t A[8];
-        uint32_t acc = 0;
-        int n = 0;
-#pragma unroll
-        for (int dy = -3; dy <= 3; dy++) {
-            const uint32_t *r = tile + (ty + 3 + dy) * RW + tx;
-            const uint32_t w0 = r[0], w1 = r[1], w2 = r[2];
-#pragma unroll
-            for (int dx = -4; dx <= 4; dx++) {
-                if (dx == 0 && dy == 0) continue;
-                acc = (acc >> 1) | (bytes_lt(window4(w0, w1, w2, 4 + dx), c, c7) & 0x80808080u);
-                if ((++n & 7) == 0) { A[(n >> 3) - 1] = acc; acc = 0; }
-            }
-        }
-        A[7] = acc >> 2;                              // bits 56..61: six compares, aligned to bit 0
-        uint64_t d[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const uint32_t sel = i | ((i + 4) << 4);
-            const uint32_t lo = __byte_perm(__byte_perm(A[0], A[1], sel), __byte_perm(A[2], A[3], sel), 0x5410);
-            const uint32_t hi = __byte_perm(__byte_perm(A[4], A[5], sel), __byte_perm(A[6], A[7], sel), 0x5410);
-            d[i] = ((uint64_t)hi << 32) | lo;
-        }
-        uint64_t *o = out + (size_t)y * W + x;
-        if (x + 3 < W) {
-            if ((((size_t)y * W + x) & 1) == 0) {
-                ((ulonglong2 *)o)[0] = make_ulonglong2(d[0], d[1]);
-                ((ulonglong2 *)o)[1] = make_ulonglong2(d[2], d[3]);
-            } else {
-#pragma unroll
-                for (int i = 0; i < 4; i++) o[i] = d[i];
-            }
-        } else {
-            for (int i = 0; i < 4 && x + i < W; i++) o[i] = d[i];
-        }
-    }
+    census_jobs<R>(tile, RW, 0, out, W, H, x0, y0, tid, nthreads);
     __syncthreads();                                  // the tile memory may be reused next
 }
 

@@ -268,8 +268,10 @@ def test_pinned_host_buffers(engine, pin):
     def pinned(a):
         t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
         return t, t.numpy()
-    for (W, H, D, paths, variant) in [(320, 200, 64, 4, sgmgb.PLAIN), (301, 77, 128, 8, sgmgb.PLAIN),
-                                      (130, 66, 64, 8, sgmgb.MULTISCALE)]:
+    cases = [(320, 200, 64, 4, sgmgb.PLAIN), (301, 77, 128, 8, sgmgb.PLAIN), (130, 66, 64, 8, sgmgb.MULTISCALE)]
+    if pin == "both":   # several tiles per block of the streaming census
+        cases.append((1920, 1080, 64, 4, sgmgb.PLAIN))
+    for (W, H, D, paths, variant) in cases:
         left, right, _ = sgmgb.synth_pair(W, H, min(D, 128), seed=W)
         want = oracle.multiscale(left, right) if variant == sgmgb.MULTISCALE else oracle.plain(left, right, D, paths)
         engine.plan(W, H, D, paths, variant)
