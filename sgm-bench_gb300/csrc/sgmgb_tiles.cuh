@@ -148,7 +148,12 @@ __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint
 // store. The population counts (2 POPC per cost) are the bound.
 // ---------------------------------------------------------------------------
 constexpr int COST_PX = 128;                          // 16 blocks of 8 pixels, or 8 of 16
-constexpr int COST_SMEM = (COST_PX + COST_PX + 256) * 8;   // bytes, 16-byte aligned by the caller
+constexpr int COST_SLW = COST_PX + COST_PX / 16;      // words of the staged left descriptors (swizzled)
+constexpr int COST_SMEM = (COST_SLW + (COST_PX + 256) + (COST_PX + 256) / 16) * 8;   // bytes, 16-byte aligned
+
+// Swizzled shared-memory word of staged descriptor j: one spare word every 16,
+// so that reads spaced by even strides spread over all 16 bank pairs.
+__device__ __forceinline__ int swz(int j) { return j + (j >> 4); }
 
 // LD_CG: read the descriptors through L2 only (the batch kernel, where other
 // blocks of the same launch wrote them); otherwise through the read-only path.
@@ -199,29 +204,78 @@ __device__ __forceinline__ void cost_tasks(const uint64_t *sl, const uint64_t *s
     }
 }
 
+// Interior tiles (no x - d < 0, no column past W) with D/8 a multiple of 4:
+// a thread makes two adjacent pixels (x, x+1) x 8 disparities from 2 left and
+// 9 right descriptors, 11 shared-memory loads for 16 costs where one pixel at
+// a time takes 18. The loads share the MIO queue with the population counts,
+// which binds this kernel. A warp covers 16 pixels x 4 groups of 8
+// disparities; for one load its lanes read words 2p - 8g + c (p < 8, g < 4),
+// which the swizzle (swz) spreads over the 16 bank pairs at most twice.
+template <bool MS>
+__device__ __forceinline__ void cost_pairs(const uint64_t *sl, const uint64_t *sr, uint8_t *__restrict__ row,
+                                           const uint8_t *__restrict__ C1, int W, int D, int y, int x0, int tid,
+                                           int nthreads) {
+    constexpr int PXW = 16;
+    constexpr int LNXB = COST_PX / PXW == 16 ? 4 : (COST_PX / PXW == 8 ? 3 : 2);   // log2(COST_PX / PXW)
+    static_assert((1 << LNXB) * PXW == COST_PX, "a tile is a power-of-two number of pixel blocks");
+    const int lane = tid & 31, pp = lane >> 2, g = lane & 3;
+    const int ntask = ((D >> 3) / 4) << LNXB;
+    const int hw = W >> 1;
+    for (int task = tid >> 5; task < ntask; task += nthreads >> 5) {
+        const int dgb = task >> LNXB, px = (task & ((1 << LNXB) - 1)) * PXW + 2 * pp;
+        const int d0 = (dgb * 4 + g) * 8, x = x0 + px;
+        const uint64_t a0 = sl[swz(px)], a1 = sl[swz(px + 1)];
+        const int base = px + (D - 1) - d0 - 7;       // r[m] = cr[x - d0 - 7 + m]
+        uint64_t r[9];
+#pragma unroll
+        for (int m = 0; m < 9; m++) r[m] = sr[swz(base + m)];
+        uint32_t v0[8], v1[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            v0[k] = (uint32_t)__popcll(a0 ^ r[7 - k]);
+            v1[k] = (uint32_t)__popcll(a1 ^ r[8 - k]);
+        }
+        if (MS) {   // full scale of the multi-scale variant: x is even, x and x+1 share (x/2, y/2)
+            const uint32_t h = *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + (x >> 1)) * D + (d0 >> 1));
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const uint32_t hk = (h >> (8 * (k >> 1))) & 0xFFu;
+                v0[k] = (v0[k] + hk + 1) >> 1;
+                v1[k] = (v1[k] + hk + 1) >> 1;
+            }
+        }
+        *(uint2 *)(row + (size_t)x * D + d0) = make_uint2(v0[0] | (v0[1] << 8) | (v0[2] << 16) | (v0[3] << 24),
+                                                          v0[4] | (v0[5] << 8) | (v0[6] << 16) | (v0[7] << 24));
+        *(uint2 *)(row + (size_t)(x + 1) * D + d0) =
+            make_uint2(v1[0] | (v1[1] << 8) | (v1[2] << 16) | (v1[3] << 24),
+                       v1[4] | (v1[5] << 8) | (v1[6] << 16) | (v1[7] << 24));
+    }
+}
+
 template <bool LD_CG, bool MS>
 __device__ __forceinline__ void cost_tile(const uint64_t *__restrict__ cl, const uint64_t *__restrict__ cr,
                                           uint8_t *__restrict__ C, const uint8_t *__restrict__ C1, int W,
                                           int D, int invalid, int y, int x0, uint8_t *smem, int tid,
                                           int nthreads) {
     uint64_t *sl = (uint64_t *)smem;                  // COST_PX left descriptors
-    uint64_t *sr = sl + COST_PX;                      // sr[j] = cr[x0 - (D-1) + j]
+    uint64_t *sr = sl + COST_SLW;                     // descriptor j: cr[x0 - (D-1) + j]
     const uint64_t *rl = cl + (size_t)y * W, *rr = cr + (size_t)y * W;
     const int nr = COST_PX + D - 1;
+    const bool dg4 = ((D >> 3) & 3) == 0;
+    const bool edge = x0 < D - 1, tail = x0 + COST_PX > W;   // uniform over the block
+    const bool pairs = dg4 && !edge && !tail;         // staged swizzled for cost_pairs
     for (int i = tid; i < COST_PX + nr; i += nthreads) {
         if (i < COST_PX) {
-            sl[i] = x0 + i < W ? ld_desc<LD_CG>(rl + x0 + i) : 0ull;
+            sl[pairs ? swz(i) : i] = x0 + i < W ? ld_desc<LD_CG>(rl + x0 + i) : 0ull;
         } else {
             const int j = i - COST_PX, x = x0 - (D - 1) + j;
-            sr[j] = (x >= 0 && x < W) ? ld_desc<LD_CG>(rr + x) : 0ull;
+            sr[pairs ? swz(j) : j] = (x >= 0 && x < W) ? ld_desc<LD_CG>(rr + x) : 0ull;
         }
     }
     __syncthreads();
     uint8_t *row = C + (size_t)y * W * D;
-    const bool dg4 = ((D >> 3) & 3) == 0;
-    const bool edge = x0 < D - 1, tail = x0 + COST_PX > W;   // uniform over the block
-    if (dg4 && !edge && !tail)
-        cost_tasks<true, MS, false, false>(sl, sr, row, C1, W, D, invalid, y, x0, tid, nthreads);
+    if (pairs)
+        cost_pairs<MS>(sl, sr, row, C1, W, D, y, x0, tid, nthreads);
     else if (dg4)
         cost_tasks<true, MS, true, true>(sl, sr, row, C1, W, D, invalid, y, x0, tid, nthreads);
     else
