@@ -205,50 +205,46 @@ __device__ __forceinline__ void cost_tasks(const uint64_t *sl, const uint64_t *s
 }
 
 // Interior tiles (no x - d < 0, no column past W) with D/8 a multiple of 4:
-// a thread makes two adjacent pixels (x, x+1) x 8 disparities from 2 left and
-// 9 right descriptors, 11 shared-memory loads for 16 costs where one pixel at
-// a time takes 18. The loads share the MIO queue with the population counts,
-// which binds this kernel. A warp covers 16 pixels x 4 groups of 8
-// disparities; for one load its lanes read words 2p - 8g + c (p < 8, g < 4),
-// which the swizzle (swz) spreads over the 16 bank pairs at most twice.
-template <bool MS>
+// a thread makes NPX adjacent pixels x 8 disparities from NPX left and NPX + 7
+// right descriptors: 11 shared-memory loads for 16 costs (NPX = 2) or 15 for
+// 32 (NPX = 4), where one pixel at a time takes 9 for 8. The loads share the
+// MIO queue with the population counts, which binds this kernel. A warp
+// covers 8 NPX pixels x 4 groups of 8 disparities; for one load its lanes
+// read words NPX p - 8g + c (p < 8, g < 4), which the swizzle (swz) spreads
+// over the 16 bank pairs.
+template <int NPX, bool MS>
 __device__ __forceinline__ void cost_pairs(const uint64_t *sl, const uint64_t *sr, uint8_t *__restrict__ row,
                                            const uint8_t *__restrict__ C1, int W, int D, int y, int x0, int tid,
                                            int nthreads) {
-    constexpr int PXW = 16;
-    constexpr int LNXB = COST_PX / PXW == 16 ? 4 : (COST_PX / PXW == 8 ? 3 : 2);   // log2(COST_PX / PXW)
+    constexpr int PXW = 8 * NPX;                      // pixels of a warp
+    constexpr int LNXB = COST_PX / PXW == 16 ? 4 : COST_PX / PXW == 8 ? 3 : COST_PX / PXW == 4 ? 2 : 1;
     static_assert((1 << LNXB) * PXW == COST_PX, "a tile is a power-of-two number of pixel blocks");
     const int lane = tid & 31, pp = lane >> 2, g = lane & 3;
     const int ntask = ((D >> 3) / 4) << LNXB;
     const int hw = W >> 1;
     for (int task = tid >> 5; task < ntask; task += nthreads >> 5) {
-        const int dgb = task >> LNXB, px = (task & ((1 << LNXB) - 1)) * PXW + 2 * pp;
+        const int dgb = task >> LNXB, px = (task & ((1 << LNXB) - 1)) * PXW + NPX * pp;
         const int d0 = (dgb * 4 + g) * 8, x = x0 + px;
-        const uint64_t a0 = sl[swz(px)], a1 = sl[swz(px + 1)];
+        uint64_t a[NPX], r[NPX + 7];
+#pragma unroll
+        for (int i = 0; i < NPX; i++) a[i] = sl[swz(px + i)];
         const int base = px + (D - 1) - d0 - 7;       // r[m] = cr[x - d0 - 7 + m]
-        uint64_t r[9];
 #pragma unroll
-        for (int m = 0; m < 9; m++) r[m] = sr[swz(base + m)];
-        uint32_t v0[8], v1[8];
+        for (int m = 0; m < NPX + 7; m++) r[m] = sr[swz(base + m)];
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-            v0[k] = (uint32_t)__popcll(a0 ^ r[7 - k]);
-            v1[k] = (uint32_t)__popcll(a1 ^ r[8 - k]);
-        }
-        if (MS) {   // full scale of the multi-scale variant: x is even, x and x+1 share (x/2, y/2)
-            const uint32_t h = *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + (x >> 1)) * D + (d0 >> 1));
+        for (int i = 0; i < NPX; i++) {
+            uint32_t v[8];
 #pragma unroll
-            for (int k = 0; k < 8; k++) {
-                const uint32_t hk = (h >> (8 * (k >> 1))) & 0xFFu;
-                v0[k] = (v0[k] + hk + 1) >> 1;
-                v1[k] = (v1[k] + hk + 1) >> 1;
+            for (int k = 0; k < 8; k++) v[k] = (uint32_t)__popcll(a[i] ^ r[7 + i - k]);
+            if (MS) {   // full scale of the multi-scale variant: x is even, pixel pairs share (x/2, y/2)
+                const uint32_t h =
+                    *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + ((x + i) >> 1)) * D + (d0 >> 1));
+#pragma unroll
+                for (int k = 0; k < 8; k++) v[k] = (v[k] + ((h >> (8 * (k >> 1))) & 0xFFu) + 1) >> 1;
             }
+            *(uint2 *)(row + (size_t)(x + i) * D + d0) = make_uint2(v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24),
+                                                                    v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24));
         }
-        *(uint2 *)(row + (size_t)x * D + d0) = make_uint2(v0[0] | (v0[1] << 8) | (v0[2] << 16) | (v0[3] << 24),
-                                                          v0[4] | (v0[5] << 8) | (v0[6] << 16) | (v0[7] << 24));
-        *(uint2 *)(row + (size_t)(x + 1) * D + d0) =
-            make_uint2(v1[0] | (v1[1] << 8) | (v1[2] << 16) | (v1[3] << 24),
-                       v1[4] | (v1[5] << 8) | (v1[6] << 16) | (v1[7] << 24));
     }
 }
 
@@ -275,7 +271,9 @@ __device__ __forceinline__ void cost_tile(const uint64_t *__restrict__ cl, const
     __syncthreads();
     uint8_t *row = C + (size_t)y * W * D;
     if (pairs)
-        cost_pairs<MS>(sl, sr, row, C1, W, D, y, x0, tid, nthreads);
+        // measured at 1080p D=64: plain 64.8 (NPX 2) / 63.9 us (NPX 4); the
+        // multi-scale merge 37.1 (NPX 2) / 43.8 us (NPX 4, 64 registers)
+        cost_pairs<MS ? 2 : 4, MS>(sl, sr, row, C1, W, D, y, x0, tid, nthreads);
     else if (dg4)
         cost_tasks<true, MS, true, true>(sl, sr, row, C1, W, D, invalid, y, x0, tid, nthreads);
     else
