@@ -48,14 +48,17 @@ static cudaError_t launch_pair_one(const LineParams &p, int wpb, cudaStream_t s)
 }
 
 // The pair layout (two lines per warp in register halves, sgmgb_pair.cuh)
-// serves the plain scratch and final-of-planes passes at D = 32, 64 and 128
-// unless a disparities-per-lane shape was asked for. (It runs every mode, with
-// saturation at D = 64, but when passes run one after another -- the sum
-// schedule -- their halved warp count costs more latency than the halved
-// instructions save; the batch kernel may still choose it for any mode.)
+// serves the scratch passes at D = 32, 64 and 128 (the multi-scale ones,
+// saturating, at D = 64) and the plain final-of-planes pass, unless a
+// disparities-per-lane shape was asked for. Alone, a pair pass is slower (half
+// the warps: multi-scale full-scale R->L 57 -> 70 us); side by side with the
+// other directions its halved instruction count wins (configuration C with 4
+// frames in flight 0.578 -> 0.535 ms). The batch kernel may choose it for any
+// mode but the eight-plane final.
 static bool pair_applies(const LineParams &p, int mode, int saturate) {
-    return p.dpl == 0 && (p.D == 32 || p.D == 64 || p.D == 128) && !saturate &&
-           (mode == MODE_SCRATCH || mode == MODE_FINAL3);
+    if (p.dpl != 0 || (p.D != 32 && p.D != 64 && p.D != 128)) return false;
+    if (mode == MODE_SCRATCH) return !saturate || p.D == 64;   // the multi-scale passes (saturating, D = 64)
+    return mode == MODE_FINAL3 && !saturate;
 }
 
 template <int NR, int SAT>
