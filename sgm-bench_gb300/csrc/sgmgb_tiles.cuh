@@ -141,11 +141,14 @@ __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint
 //                 at (x/2, y/2, d/2): (c2 + c1 + 1) >> 1                 (multiscale/sgm_ms_ref.c:184-188)
 // The row's left descriptors and the right ones from D-1 columns before the
 // tile are staged in shared memory. A thread makes 8 consecutive disparities
-// of one pixel and stores them as one 8-byte word. A warp covers 8 pixels x 4
-// disparity groups (16 x 2 when D/8 is not a multiple of 4): its 32 right-
-// descriptor reads for one k are then 32 consecutive words (no bank
-// conflicts), and each pixel's 32 bytes of the warp are one sector in the
-// store. The population counts (2 POPC per cost) are the bound.
+// of a pixel and stores them as one 8-byte word; a warp covers 4 groups of 8
+// disparities (2 when D/8 is not a multiple of 4), so each pixel's 32 bytes of
+// the warp are one sector in the store. Interior tiles (most of them) take
+// cost_pairs: several adjacent pixels per thread from a swizzled staging
+// layout, which cuts the shared-memory loads that share the MIO queue with
+// the population counts (2 POPC per cost). Edge tiles (x - d < 0, columns past
+// W) take cost_tasks: one pixel per thread, 8 pixels x 4 groups per warp, so
+// that its 32 right-descriptor reads for one k are 32 consecutive words.
 // ---------------------------------------------------------------------------
 constexpr int COST_PX = 128;                          // 16 blocks of 8 pixels, or 8 of 16
 constexpr int COST_SLW = COST_PX + COST_PX / 16;      // words of the staged left descriptors (swizzled)
