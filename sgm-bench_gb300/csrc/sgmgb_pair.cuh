@@ -38,15 +38,16 @@ namespace {
 // K = 8 G / NR steps. The scratch passes (one input stream) take chunks of
 // 1 KB (2 KB at D = 128): fewer per-chunk waits, copies and stores per step
 // (measured at D = 64: 512 B 125 us, 1 KB 94 us, 2 KB 98 us per row pass; at
-// D = 128: 1 KB 167 us, 2 KB 143 us). The other modes keep 512 bytes, which
-// bounds their shared memory: 1 KB chunks made the T->B final pass 166 ->
-// 152 us alone, but its ring (four streams) then takes 96 KB per 4-warp block
-// and four frames in flight went 0.280 -> 0.292 ms per frame.
+// D = 128: 1 KB 167 us, 2 KB 143 us). The final-of-planes pass (four input
+// streams) takes 1 KB chunks in a ring of three: 166 -> 151 us alone, and the
+// ring stays at 48 KB per 4-warp block (a ring of six, 96 KB, had made four
+// frames in flight slower: 0.280 -> 0.292 ms per frame; with three, 0.268 ->
+// 0.261). The other modes keep 512 bytes.
 template <int NR, int MODE> struct PairRing {
-    static constexpr int G = MODE == MODE_SCRATCH ? (NR == 4 ? 4 : 2) : 1;   // granules per lane per stream
+    static constexpr int G = MODE == MODE_SCRATCH ? (NR == 4 ? 4 : 2) : (MODE == MODE_FINAL3 ? 2 : 1);
     static constexpr int CB = 512 * G;                             // bytes of one stream per chunk
     static constexpr int K = 8 * G / NR;                           // steps per chunk
-    static constexpr int NCH = NR == 1 ? 4 : (NR == 2 ? 6 : 8);    // ring depth in chunks
+    static constexpr int NCH = MODE == MODE_FINAL3 ? 3 : (NR == 1 ? 4 : (NR == 2 ? 6 : 8));   // ring depth
     static constexpr int SB = 64 * NR;                             // bytes of one stream per step: [A | B]
 };
 // Streams of a chunk slot, in units of CB bytes: the cost bytes, the planes
