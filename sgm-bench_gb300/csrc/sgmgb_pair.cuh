@@ -149,6 +149,10 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     line_start(P, la, xa, ya, lena);
     line_start(P, la + 1, xb, yb, lenb);              // lenb = 0 if there is no second line
     const int maxlen = max(lena, lenb), minlen = lenb ? min(lena, lenb) : lena;
+    // final passes down or up the columns: the two lines are adjacent columns
+    // of equal length, so their two disparities of a step are one 16-bit store
+    const bool pair_store = P.dx == 0 && lenb == lena && ((ya * P.W + xa) & 1) == 0 && (P.W & 1) == 0 &&
+                            xb == xa + 1 && yb == ya && ((uintptr_t)P.disp & 1) == 0;
     const int dx = P.dx, dy = P.dy, step = dy * P.W + dx;
     int pa = ya * P.W + xa, pb = yb * P.W + xb;
     const uint32_t P1 = pk2((uint32_t)P.p1), P2 = pk2((uint32_t)P.p2);
@@ -303,6 +307,8 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             if (MODE == MODE_FINAL && P.even_only) {  // multi-scale: the map at (2x, 2y) only
                 if (live_a && !((xa | ya) & 1)) P.disp[(long long)(ya >> 1) * hw + (xa >> 1)] = (uint8_t)da;
                 if (live_b && !((xb | yb) & 1)) P.disp[(long long)(yb >> 1) * hw + (xb >> 1)] = (uint8_t)db;
+            } else if (pair_store) {
+                if (live_a) *(uint16_t *)(P.disp + pa) = (uint16_t)(da | (db << 8));
             } else {
                 if (live_a) P.disp[pa] = (uint8_t)da;
                 if (live_b) P.disp[pb] = (uint8_t)db;
