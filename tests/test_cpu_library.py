@@ -33,6 +33,23 @@ def test_every_declared_symbol_is_exported():
         assert hasattr(lib, name), name
 
 
+def test_header_constants_match_the_binding():
+    """The #define values of the C header and the Python binding's constants
+    (variants, schedules, error codes) are the same numbers."""
+    src = open(os.path.join(ROOT, "include", "sgmgb.h")).read()
+    defines = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(SGMGB_\w+)\s+(-?\d+)", src)}
+    assert defines["SGMGB_SCHED_AUTO"] == sgmgb.SCHED_AUTO
+    assert defines["SGMGB_SCHED_LATENCY"] == sgmgb.SCHED_LATENCY
+    assert defines["SGMGB_SCHED_THROUGHPUT"] == sgmgb.SCHED_THROUGHPUT
+    enums = {m.group(1): int(m.group(2)) for m in re.finditer(r"(SGMGB_\w+)\s*=\s*(-?\d+)", src)}
+    for name, value in (("SGMGB_OK", sgmgb.OK), ("SGMGB_ERR_ARG", sgmgb.ERR_ARG), ("SGMGB_ERR_NOMEM", sgmgb.ERR_NOMEM),
+                        ("SGMGB_ERR_CUDA", sgmgb.ERR_CUDA), ("SGMGB_ERR_NODEV", sgmgb.ERR_NODEV),
+                        ("SGMGB_ERR_BUDGET", sgmgb.ERR_BUDGET), ("SGMGB_ERR_TIMEOUT", sgmgb.ERR_TIMEOUT),
+                        ("SGMGB_ERR_STATE", sgmgb.ERR_STATE), ("SGMGB_PLAIN", sgmgb.PLAIN),
+                        ("SGMGB_MULTISCALE", sgmgb.MULTISCALE)):
+        assert (enums.get(name) if name in enums else defines.get(name)) == value, name
+
+
 @pytest.mark.parametrize("D,paths", [(64, 4), (128, 4), (64, 8), (128, 8)])
 def test_plugin_exports_sgm_impl(D, paths):
     p = sgmgb.Plugin(D, paths)
