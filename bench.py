@@ -10,18 +10,25 @@ inputs already resident on the device (one CUDA-graph launch per frame,
 round-robin over 8 distinct synthetic pairs whose working set is far larger
 than L2); `e2e` is the same metric through the host-buffer call
 (sgmgb_run_frame: pinned host inputs copied in, the disparity map copied
-back, every step). `roofline` is the dominant kernel's: its algorithmic bytes
-per launch over its mean launch time (CUDA events, kernel alone), against the
-measured HBM copy bandwidth; `frame_roofline` relates the modelled minimal
-bytes of a frame (2*W*H*D + 3*W*H) to the pipelined frame time. `batched`
-runs the 96-pair mixed batch in one persistent launch against 96 sequential
-drop-in calls; `served` drives 8 virtual cameras with Poisson arrivals at
-2000 frames/s through the server and reports p50/p99 latency.
-`multiscale` times configurations B and C (the multi-scale 8-path variant at
-1920x800 and 1920x1080). `cpu_baseline` is the CPU oracle on a bounded sample of
-the same workload, one thread; that leg is also where the oracle checks the
-GPU's maps (`bit_exact_vs_oracle`). `--impl reference` times the CPU oracle
-(the reference's algorithm, restated in C) on all host threads.
+back, every step), and `e2e.pageable` through the plugin's SGM_IMPL.run on
+pageable buffers, as the reference harness calls it. `roofline` is the
+dominant kernel's: its algorithmic bytes per launch over its mean launch time
+(CUDA events, kernel alone), against the measured HBM copy bandwidth;
+`frame_roofline` relates the modelled minimal bytes of a frame
+(2*W*H*D + 3*W*H) to the pipelined frame time. `batched` runs the 96-pair
+mixed batch in one persistent launch against 96 sequential drop-in calls;
+`served` drives 8 virtual cameras with Poisson arrivals through the server
+and reports p50/p99 latency. `multiscale` times configurations B and C (the
+multi-scale 8-path variant at 1920x800 and 1920x1080).
+
+The CPU leg runs last: `cpu_baseline` is the reference's own common/sgm_ref.c
+(built from its sources by oracle/build_ref.sh and called through its
+SGM_IMPL; the oracle port where it is not built) on whole frames, one
+thread; the same run checks the GPU's maps (`bit_exact`), the reference's
+multi-scale program checks and times configurations B/C on every host thread,
+and one frame of each class of the batched mix is checked against the
+reference. `--impl reference` times the reference's CPU path on every host
+thread, one whole frame per thread per step, with the same `config`.
 
 Multi-GPU: frames are independent, so N GPUs run N replicas (one process per
 GPU under torchrun); `value` is the frames of all ranks over the slowest
@@ -35,6 +42,8 @@ import subprocess
 import sys
 import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 for p in (os.path.join(ROOT, "sgm-bench_gb300"), os.path.join(ROOT, "oracle")):
@@ -187,20 +196,31 @@ def batched_section(eng_cls, sgmgb, torch, np):
     for sp, (l, r) in zip(specs, host):
         engs[sp].run_frame(l, r)
     seq_ms = (time.perf_counter() - t0) * 1e3
-    same = all(np.array_equal(o.cpu().numpy(), rf) for o, rf in zip(out, ref))
+    maps = [o.cpu().numpy() for o in out]
+    same = all(np.array_equal(m, rf) for m, rf in zip(maps, ref))
     shapes = sorted(set(b.tile_shape(i) for i in range(len(specs))))
     for e in engs.values():
         e.close()
     b.close()
     eng.close()
+    # one frame of every (size, D, paths) class for the CPU leg's reference
+    # check; frames of a class share the class's input pair, so a class whose
+    # maps are all identical is covered by its one checked frame
+    checks, seen, covered = [], {}, 0
+    for sp, (l, r), m in zip(specs, host, maps):
+        if sp not in seen:
+            seen[sp] = m
+            checks.append(sp + (l, r, m))
+        covered += int(np.array_equal(m, seen[sp]))
     mde = sum(W * H * Dk for (W, H, Dk, P) in specs)
     return {"frames": len(specs), "ms_per_batch": batch_ms, "fps": 96e3 / batch_ms,
             "mde_per_s": mde / (batch_ms / 1e3) / 1e6,
             "sequential_dropin_ms": seq_ms, "sequential_dropin_fps": 96e3 / seq_ms,
             "speedup_vs_sequential_dropin": seq_ms / batch_ms, "identical_to_dropin": bool(same),
+            "frames_equal_to_their_checked_class_frame": covered,
             "launches_per_batch": 1, "tile_shapes_warps_dpl": shapes,
             "note": "one persistent launch per batch (CUDA graph); batch inputs resident on the device; "
-                    "drop-in calls copy host buffers in and out"}
+                    "drop-in calls copy host buffers in and out"}, checks
 
 
 def served_section(eng_cls, sgmgb, np, rate=2000.0, secs=3.0):
@@ -274,26 +294,64 @@ def served_section(eng_cls, sgmgb, np, rate=2000.0, secs=3.0):
             "latency": "submit (host copy into pinned memory) to result in pinned host memory"}
 
 
-def cpu_baseline_sample(seconds, left, right, gpu_maps, ms_checks=()):
-    """The CPU leg: the oracle (the reference's scalar algorithm restated in C),
-    one thread, timed on whole frames of the workload -- the very pair the GPU
-    timed first -- and used as the checker of the GPU's maps: `gpu_maps` are the
-    maps every timed context made of that pair, `ms_checks` (left, right, map)
-    multi-scale maps of the multiscale section."""
-    import numpy as np
+def cpu_baseline_sample(seconds, left, right, gpu_maps, ms_checks=(), batch_checks=()):
+    """The CPU leg, run after every GPU section.
+
+    cpu_baseline: the reference's own common/sgm_ref.c (its SGM_IMPL, built from
+    its sources; the oracle port where it was not built), one thread, as the
+    reference runs it (single-threaded by design, sgm_ref.c:3), timed on whole
+    configuration-A frames -- the pair the GPU timed first -- for at most
+    `seconds` (8 frames at most).
+
+    The checker: the GPU's maps of that pair (`gpu_maps`) against that output;
+    the multi-scale maps (`ms_checks`: name, left, right, map) against
+    multiscale/sgm_ms_ref.c run on every host thread (its FNV hash; that run is
+    also the multi-scale CPU baseline), else the oracle; and one frame of every
+    (size, D, paths) class of the batched mix (`batch_checks`: W, H, D, paths,
+    left, right, map) against the reference for that D and path count, on a
+    thread pool."""
+    import concurrent.futures as cf
     import oracle
+    run, kind = reference_checker(D, PATHS)
     n, t0 = 0, time.perf_counter()
     while True:
-        want = oracle.plain(left, right, D, PATHS)
+        want = run(left, right)
         n += 1
         el = time.perf_counter() - t0
         if el >= seconds or n >= 8:
             break
     exact = all(np.array_equal(m, want) for m in gpu_maps)
-    ms_exact = all(np.array_equal(m, oracle.multiscale(l, r)) for l, r, m in ms_checks) if ms_checks else None
-    return {"value": n * W * H * D / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "%d frame(s) of %dx%d D=%d %d-path, oracle/sgm_oracle.c, 1 thread, %.1f s"
-                      % (n, W, H, D, PATHS, el)}, exact, ms_exact
+    what = "common/sgm_ref.c via SGM_IMPL" if kind == "reference" else "oracle/sgm_oracle.c"
+    base = {"value": n * W * H * D / el / 1e6, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": "%d frame(s) of %dx%d D=%d %d-path, %s, 1 thread, %.1f s" % (n, W, H, D, PATHS, what, el)}
+    ms = {}
+    for name, l, r, m in ms_checks:
+        Wm, Hm = l.shape[1], l.shape[0]
+        work = ((Wm // 2) * (Hm // 2) + Wm * Hm) * 64
+        try:
+            med, fnv, omp, thr = oracle.reference_multiscale(l, r, reps=3)
+            ms[name] = {"bit_exact_vs_reference": fnv == oracle.fnv1a64(m),
+                        "cpu_baseline": {"ms_per_frame": med, "mde_per_s_work": work / (med / 1e3) / 1e6,
+                                         "cores": thr, "kind": "reference", "openmp": omp,
+                                         "sample": "3 frames, multiscale/sgm_ms_ref.c (median it prints), "
+                                                   "OMP_NUM_THREADS=%d" % thr}}
+        except FileNotFoundError:
+            ms[name] = {"bit_exact_vs_oracle": bool(np.array_equal(m, oracle.multiscale(l, r)))}
+    batch = None
+    if batch_checks:
+        threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+        def one(c):
+            Wc, Hc, Dc, Pc, l, r, m = c
+            f, k = reference_checker(Dc, Pc)
+            return bool(np.array_equal(f(l, r), m)), k
+
+        with cf.ThreadPoolExecutor(max_workers=min(threads, len(batch_checks))) as pool:
+            res = list(pool.map(one, batch_checks))
+        batch = {"classes_checked": len(res), "all_exact": all(r[0] for r in res),
+                 "kinds": sorted(set(r[1] for r in res)),
+                 "failed": ["%dx%d D=%d P=%d" % c[:4] for c, r in zip(batch_checks, res) if not r[0]]}
+    return base, exact, ms, batch
 
 
 def sweep_section(sgmgb, torch, np, warmup=10, frames=60):
@@ -351,7 +409,7 @@ def multiscale_section(sgmgb, torch, np, steps=60, inflight=4):
             engs[i % inflight].run_frame_async(dl[i % inflight], dr[i % inflight], dd[i % inflight],
                                                stream=strs[i % inflight])
         torch.cuda.synchronize()
-        checks.append((pairs[0][0], pairs[0][1], dd[0].cpu().numpy()))
+        checks.append((name, pairs[0][0], pairs[0][1], dd[0].cpu().numpy()))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0 = strs[0]
         e0.record(s0)
@@ -388,42 +446,63 @@ def multiscale_section(sgmgb, torch, np, steps=60, inflight=4):
     return out, checks
 
 
+def workload_config(ws):
+    """The `config` both arms print: the workload, not how an arm runs it."""
+    return {"workload": WORKLOAD, "W": W, "H": H, "D": D, "paths": PATHS, "variant": "plain",
+            "inputs": "8 synthetic pairs (seeds 1..8) round-robin; per-frame working set > L2",
+            "parallelism": "replicas" if ws > 1 else "single"}
+
+
+def reference_checker(Dk, paths):
+    """(function left, right -> map, kind): the reference's own sgm_ref.c built
+    from its sources (oracle/_ref) where it was built, else the oracle port."""
+    import oracle
+    if oracle.reference_available(Dk, paths):
+        ref = oracle.ReferenceImpl(Dk, paths)
+        return ref.run, "reference"
+    return (lambda l, r: oracle.plain(l, r, Dk, paths)), "port"
+
+
 def run_reference(args):
-    """The reference's CPU algorithm (oracle port) on every host thread."""
+    """The reference's CPU implementation of the path (common/sgm_ref.c through
+    its SGM_IMPL, built from its sources by oracle/build_ref.sh; the oracle port
+    where it is not built) on every host thread: each step, every thread runs
+    one whole configuration-A frame (single-threaded by design, sgm_ref.c:3),
+    so a step is `threads` frames. Long runs (steps + warmup > 40) time a band
+    of rows per frame instead, to end within minutes. Rank 0 only."""
     ws, rank, _ = dist_setup()
     if rank != 0:
         return 0
     import concurrent.futures as cf
     import oracle
-    import sgmgb
     threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
-    # each step: every thread runs one band of the frame (a full frame when the
-    # run is short); rows scale down so the whole run stays within minutes.
-    rows = max(64, min(H, int(H * 16 / max(16, args.steps + args.warmup))))
-    pairs = [sgmgb.synth_pair(W, H, D, 200 + t) for t in range(threads)]
-    bands = [(l[:rows].copy(), r[:rows].copy()) for l, r, _ in pairs]
+    run, kind = reference_checker(D, PATHS)
+    total = args.steps + args.warmup
+    rows = H if total <= 40 else max(64, int(H * 40 / total))
+    pairs = [oracle.synth_pair(W, H, D, k + 1)[:2] for k in range(8)]
+    work = [(np.ascontiguousarray(l[:rows]), np.ascontiguousarray(r[:rows])) for l, r in pairs]
     pool = cf.ThreadPoolExecutor(max_workers=threads)
 
-    def step():
-        list(pool.map(lambda lr: oracle.plain(lr[0], lr[1], D, PATHS), bands))
+    def step(i):
+        list(pool.map(lambda t: run(*work[(i * threads + t) % 8]), range(threads)))
 
-    for _ in range(args.warmup):
-        step()
+    for i in range(args.warmup):
+        step(i)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step()
+    for i in range(args.steps):
+        step(args.warmup + i)
     el = time.perf_counter() - t0
     per_step = el / args.steps
     value = threads * W * rows * D / per_step / 1e6
-    sample = "%d threads x one %dx%d D=%d %d-path band per step (oracle port of common/sgm_ref.c)" % (
-        threads, W, rows, D, PATHS)
+    what = "common/sgm_ref.c via SGM_IMPL" if kind == "reference" else "oracle port of common/sgm_ref.c"
+    sample = "%d threads x one %dx%d D=%d %d-path %s per step (%s)" % (
+        threads, W, rows, D, PATHS, "frame" if rows == H else "band of the frame", what)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "W": W, "H": H, "D": D, "paths": PATHS,
-                       "sample_rows": rows, "threads": threads},
+            "config": workload_config(ws),
             "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -540,6 +619,27 @@ def run_gb300(args):
     _, st = eng.run_frame(hl[0], hr[0], times=True, out=ho[0])
     e2e_exact = bool(np.array_equal(ho[0], maps0[0]))   # the map that came back is the timed frame's map
 
+    # the drop-in exactly as the reference harness calls it (common/harness.c:
+    # 142-158): the plugin's SGM_IMPL.run on ordinary pageable buffers, with a
+    # fresh zeroed map per call, so the copies go through the copy engines
+    plug = sgmgb.Plugin(D, PATHS)
+    pl = [np.array(p[0]) for p in pairs]
+    pr = [np.array(p[1]) for p in pairs]
+    for i in range(3):
+        plug.run(pl[i % R], pr[i % R])
+    if dist is not None:
+        dist.barrier()
+    lat_pg = []
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        a = time.perf_counter()
+        rc, pmap, _ = plug.run(pl[i % R], pr[i % R])
+        lat_pg.append(time.perf_counter() - a)
+        if rc:
+            raise RuntimeError("SGM_IMPL.run failed")
+    pg_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    pg_exact = bool(np.array_equal(plug.run(pl[0], pr[0])[1], maps0[0]))
+
     # per-kernel device time, each kernel alone, CUDA events on the engine's
     # stream: the throughput schedule (`value`) and the latency one (`e2e`)
     eng.set_schedule(sgmgb.SCHED_THROUGHPUT)
@@ -563,13 +663,12 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u16", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "W": W, "H": H, "D": D, "paths": PATHS, "variant": "plain",
-                   "inputs": "8 resident synthetic pairs round-robin; per-frame working set 570 MB > L2",
-                   "frames_in_flight": NF, "schedule": "throughput (frames in flight)",
-                   "parallelism": "replicas" if ws > 1 else "single"},
+        "config": workload_config(ws),
+        "run": {"frames_in_flight": NF, "schedule": "throughput (frames in flight)",
+                "inputs": "resident on the device; per-frame working set 570 MB > L2"},
         "frame_latency_ms": serial_ms_per_frame,
         "fps": ws * args.steps / (ms / 1e3),
-        "bit_exact_vs_oracle": None,
+        "bit_exact": None,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * W * H, "d2h_bytes_per_step": W * H,
                 "fps": ws * e2e_steps / e2e_s, "p50_ms": statistics.median(lat) * 1e3,
                 "p99_ms": sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
@@ -578,6 +677,13 @@ def run_gb300(args):
                 "transfers": "pinned host buffers: the first kernel reads both images and the sum pass writes the "
                              "map across NVLink-C2C inside the call",
                 "same_map_as_device_path": e2e_exact,
+                "pageable": {"value": replica_value(ws, e2e_steps, pg_s), "unit": UNIT,
+                             "fps": ws * e2e_steps / pg_s, "p50_ms": statistics.median(lat_pg) * 1e3,
+                             "p99_ms": sorted(lat_pg)[min(len(lat_pg) - 1, int(0.99 * len(lat_pg)))] * 1e3,
+                             "h2d_bytes_per_step": 2 * W * H, "d2h_bytes_per_step": W * H,
+                             "call": "SGM_IMPL.run of libsgm_gb300_d64_p4.so, pageable numpy buffers, a new "
+                                     "zeroed map per call, as common/harness.c:142-158",
+                             "same_map_as_device_path": pg_exact},
                 "kernels_alone_ms": {k[0]: round(k[1], 5) for k in kstats_lat}},
         "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": top[2],
@@ -598,19 +704,24 @@ def run_gb300(args):
     }
     for e in engines:
         e.close()
-    ms_checks = ()
+    ms_checks, batch_checks = (), ()
     if not args.no_multiscale:
         line["multiscale"], ms_checks = multiscale_section(sgmgb, torch, np)
-    line["cpu_baseline"], line["bit_exact_vs_oracle"], ms_exact = cpu_baseline_sample(
-        args.cpu_seconds, pairs[0][0], pairs[0][1], maps0, ms_checks)
-    if ms_exact is not None:
-        line["multiscale"]["bit_exact_vs_oracle"] = ms_exact
     if not args.no_sweep:
         line["d_sweep"] = sweep_section(sgmgb, torch, np)
     if not args.no_batch:
-        line["batched"] = batched_section(sgmgb.Engine, sgmgb, torch, np)
+        line["batched"], batch_checks = batched_section(sgmgb.Engine, sgmgb, torch, np)
     if not args.no_serve:
         line["served"] = served_section(sgmgb.Engine, sgmgb, np)
+    base, exact, ms_res, batch_res = cpu_baseline_sample(args.cpu_seconds, pairs[0][0], pairs[0][1], maps0,
+                                                         ms_checks, batch_checks)
+    line["cpu_baseline"] = base
+    line["bit_exact"] = {"value": exact, "checker": base["kind"],
+                         "what": "every timed context's map of the first pair vs the checker's map"}
+    for name, r in ms_res.items():
+        line["multiscale"][name].update(r)
+    if batch_res is not None:
+        line["batched"]["reference_check"] = batch_res
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -152,21 +152,28 @@ int sgmgb_census_async(sgmgb_ctx *ctx, const uint8_t *d_img, uint64_t *d_out, in
 /* No counterpart in the reference. Runs one plain-variant frame on device
  * buffers on `stream` (a cudaStream_t; NULL = the legacy default stream),
  * with its whole workspace -- census descriptors, cost volume and three
- * W*H*D planes, 16*W*H + 4*W*H*D bytes -- in one static device array of
- * SGMGB_NOALLOC_SCRATCH_BYTES (24 MiB), so it allocates nothing: no device,
- * host or library allocation. It is for callers that must not allocate after
- * start-up, such as a real-time loop with a fixed device-memory budget, where
- * cudaMalloc/cudaFree can block on device-wide synchronisation or fail once
- * another allocator holds the free memory. Limit: the workspace must fit the
- * array, e.g. 320x240 at D=64 (4 or 8 paths), 200x200 at D=128, 640x480 at
- * D=16; larger frames return SGMGB_ERR_BUDGET. The first call on a device
- * looks up the array's address (cudaGetSymbolAddress, with that device
- * current) and sets the path kernels' shared-memory limits, so make the first
- * call before any stream capture. Nothing in the array needs to start at
- * zero: every byte a call reads is written earlier in the same call, in
- * stream order. All calls on a device share the one array: calls that overlap
- * in time (on other streams or threads) race and corrupt each other's output,
- * so serialise them, e.g. on one stream. Returns SGMGB_OK, SGMGB_ERR_ARG,
+ * W*H*D planes: 16*W*H + 4*W*H*D bytes in five regions, each rounded up to a
+ * multiple of 256 bytes (at most 5*255 bytes more) -- in one static device
+ * array of SGMGB_NOALLOC_SCRATCH_BYTES (24 MiB), so it allocates nothing: no
+ * device, host or library allocation. It is for callers that must not
+ * allocate after start-up, such as a real-time loop with a fixed
+ * device-memory budget, where cudaMalloc/cudaFree can block on device-wide
+ * synchronisation or fail once another allocator holds the free memory.
+ * Limit: the workspace must fit the array, e.g. 320x240 at D=64 (4 or 8
+ * paths), 200x200 at D=128, 640x480 at D=16; larger frames return
+ * SGMGB_ERR_BUDGET. It runs on the CUDA device current in the calling thread
+ * (the buffers must be that device's); note that the context calls above
+ * (sgmgb_run_frame, sgmgb_batch_run, ...) make their context's device current
+ * and leave it so. The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress, with that device current) and sets the path kernels'
+ * shared-memory limits (cudaFuncSetAttribute), so make the first call before
+ * any stream capture. Every call makes these CUDA runtime calls: cudaGetDevice,
+ * then one launch per kernel (6 for 4 paths, 10 for 8), each followed by
+ * cudaGetLastError. Nothing in the array needs to start at zero: every byte
+ * a call reads is written earlier in the same call, in stream order. All
+ * calls on a device share the one array: calls that overlap in time (on
+ * other streams or threads) race and corrupt each other's output, so
+ * serialise them, e.g. on one stream. Returns SGMGB_OK, SGMGB_ERR_ARG,
  * SGMGB_ERR_BUDGET, SGMGB_ERR_NODEV or SGMGB_ERR_CUDA (launch failure). */
 int sgmgb_run_frame_noalloc(const uint8_t *d_left, const uint8_t *d_right, uint8_t *d_disp,
                             int W, int H, int D, int paths, void *stream);

@@ -5,8 +5,9 @@
 // SGMGB_NOALLOC_SCRATCH_BYTES; the kernels are the engine's own census, cost
 // and path kernels, launched one after another on the caller's stream. Its
 // address comes from cudaGetSymbolAddress, looked up once per device (with
-// that device current) together with the path kernels' shared-memory limits;
-// after that a call makes no CUDA runtime call other than kernel launches.
+// that device current) together with the path kernels' shared-memory limits.
+// Every call then makes cudaGetDevice, its kernel launches, and one
+// cudaGetLastError after each launch -- no other CUDA runtime call.
 #include "sgmgb_internal.h"
 #include <mutex>
 

@@ -454,6 +454,20 @@ int sgmgb_plan(sgmgb_ctx *ctx, const sgmgb_frame_desc *fd) {
     if (rc) return set_err(ctx, rc, err);
     ctx->fd = *fd;
     ctx->planned = true;
+    // One frame of each schedule on the slot's own zeroed buffers, so every
+    // kernel variant the description runs is loaded here (lazy module
+    // loading) and not inside the first frame's stage times.
+    const FrameSlot &s = *ctx->slot;
+    const size_t N = (size_t)fd->W * fd->H;
+    cudaError_t e = cudaMemsetAsync(s.left, 0, N, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.right, 0, N, ctx->stream);
+    for (int sched : {SGMGB_SCHED_LATENCY, SGMGB_SCHED_THROUGHPUT}) {
+        PathShape sh = ctx->shape;
+        sh.sched = sched;
+        if (e == cudaSuccess) e = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, sh, nullptr, nullptr);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "plan (kernel warm-up)");
     return SGMGB_OK;
 }
 

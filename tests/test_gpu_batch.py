@@ -131,3 +131,31 @@ def test_batch_rejects_bad_input(engine):
     with pytest.raises(sgmgb.SgmError):
         b.run([0], [0], [0])
     b.close()
+
+
+def test_batch_baseline_sizes(engine, baseline_frames):
+    """One persistent launch over frames at the batched configuration's sizes
+    (1920x1080 D=128 8-path, 1920x800 D=64 8-path, 1280x720 D=128 4-path),
+    every map byte for byte against the checker, on two runs."""
+    import torch
+    keys = list(baseline_frames)
+    descs = [sgmgb.desc(*k) for k in keys]
+    dl = [torch.from_numpy(baseline_frames[k][0]).cuda() for k in keys]
+    dr = [torch.from_numpy(baseline_frames[k][1]).cuda() for k in keys]
+    outs = [torch.zeros((k[1], k[0]), dtype=torch.uint8, device="cuda") for k in keys]
+    b = sgmgb.Batch(engine, descs)
+    try:
+        for run in range(2):
+            for o in outs:
+                o.zero_()
+            b.run(dl, dr, outs)
+            b.wait()
+            torch.cuda.synchronize()
+            for k, o in zip(keys, outs):
+                got, want = o.cpu().numpy(), baseline_frames[k][2]
+                if not np.array_equal(got, want):
+                    y, x = np.argwhere(got != want)[0]
+                    pytest.fail("run %d %r: %d pixels differ, first (x=%d,y=%d) got %d want %d"
+                                % (run, k, int((got != want).sum()), x, y, got[y, x], want[y, x]))
+    finally:
+        b.close()

@@ -286,3 +286,28 @@ def test_pinned_host_buffers(engine, pin):
         for _ in range(2):
             got = engine.run_frame(left, right, out=out)
             assert np.array_equal(got, want), (W, H, D, paths, variant, pin)
+
+
+# ---- frames at the batched and served configurations' sizes ----
+@pytest.mark.parametrize("sched", ["latency", "throughput"])
+@pytest.mark.parametrize("frame", [(1920, 1080, 128, 8), (1920, 800, 64, 8)])
+def test_baseline_size_8path(engine, baseline_frames, sched, frame):
+    """Plain 8-path at full size (long diagonals of up to 1080 steps, the
+    eight-plane final pass of the throughput schedule) through the host-buffer
+    and the device-buffer calls, byte for byte against the checker."""
+    import torch
+    left, right, want = baseline_frames[frame]
+    W, H, D, paths = frame
+    engine.set_schedule(sgmgb.SCHED_LATENCY if sched == "latency" else sgmgb.SCHED_THROUGHPUT)
+    try:
+        engine.plan(W, H, D, paths)
+        got = engine.run_frame(left, right)
+        assert np.array_equal(got, want), _first_diff(got, want)
+        dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
+        dd = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+        engine.run_frame_async(dl, dr, dd)
+        engine.sync()
+        got = dd.cpu().numpy()
+        assert np.array_equal(got, want), "async:" + _first_diff(got, want)
+    finally:
+        engine.set_schedule(sgmgb.SCHED_AUTO)

@@ -62,3 +62,29 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     with contextlib.redirect_stdout(buf):
         assert bench.run_reference(A()) == 0
     assert buf.getvalue() == ""                         # no work, no line on the other ranks
+
+
+def test_reference_arm_line_matches_the_gpu_arm_config(monkeypatch):
+    """The reference arm prints one line on rank 0 with the GPU arm's `config`
+    (the driver compares the two), its CPU baseline and a zero-copy e2e; a
+    small frame stands in for configuration A so the test runs in seconds."""
+    sys.path.insert(0, ROOT)
+    import json
+    import bench
+    monkeypatch.setattr(bench, "W", 96)
+    monkeypatch.setattr(bench, "H", 40)
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+
+    class A:
+        steps, warmup, gpus = 2, 1, 1
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        assert bench.run_reference(A()) == 0
+    line = json.loads(buf.getvalue())
+    assert line["impl"] == "reference" and line["steps"] == 2 and line["warmup"] == 1
+    assert line["config"] == bench.workload_config(1)
+    assert line["cpu_baseline"]["value"] == line["value"] > 0
+    assert line["cpu_baseline"]["kind"] in ("reference", "port")
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}

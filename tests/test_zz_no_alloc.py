@@ -1,8 +1,12 @@
 """sgmgb_run_frame_noalloc: a plain frame whose workspace is a static device
 array (no allocation), checked through the C ABI against the allocating
-entry point sgmgb_run_frame_async on two calls in a row. The file name sorts
-last so that it runs after every other test, and it needs no fixture from
-them, so it also runs alone."""
+entry point sgmgb_run_frame_async on two calls in a row, and both against the
+oracle. The cases cover 4 and 8 paths at D = 16, 32, 64 and 128: the 8-path
+chain's first pass of each pair runs in the two-lines-per-warp layout at
+D = 32, 64 and 128 and the one-line layout at D = 16, its sum passes
+(S = sc + L, S += sc + L, argmin of S + sc + L) in the one-line layout. The
+file name sorts last so that it runs after every other test, and it needs no
+fixture from them, so it also runs alone."""
 import numpy as np
 import pytest
 
@@ -11,7 +15,8 @@ import sgmgb
 
 pytestmark = pytest.mark.gpu
 
-CASES = [(320, 240, 64, 4), (200, 120, 64, 8), (200, 200, 128, 4), (97, 45, 16, 8), (1, 1, 64, 4)]
+CASES = [(320, 240, 64, 4), (200, 120, 64, 8), (200, 200, 128, 4), (97, 45, 16, 8), (1, 1, 64, 4),
+         (160, 90, 32, 8), (200, 200, 128, 8)]
 
 
 def _noalloc(dl, dr, out, W, H, D, paths):
@@ -35,8 +40,8 @@ def test_noalloc_equals_run_frame_async_twice():
             assert _noalloc(dl, dr, out, W, H, D, paths) == sgmgb.OK
             torch.cuda.synchronize()
             assert torch.equal(out, ref), "%dx%d D=%d paths=%d call %d" % (W, H, D, paths, call)
-        if W * H <= 320 * 240 and D == 64:
-            assert np.array_equal(ref.cpu().numpy(), oracle.plain(left, right, D, paths))
+        # and both against the oracle directly
+        assert np.array_equal(ref.cpu().numpy(), oracle.plain(left, right, D, paths)), (W, H, D, paths)
     eng.close()
 
 
