@@ -3,6 +3,7 @@ contract for `ms`; `plain` and `gen` beside it). PGM files in and out, the
 result line with the FNV hash, exit status 2 on a golden mismatch."""
 import json
 import os
+import re
 import subprocess
 
 import numpy as np
@@ -115,3 +116,67 @@ def test_cli_plain_golden(tmp_path, D, paths):
     assert p.returncode == 0, p.stdout + p.stderr
     assert p.stdout.startswith("gb300  in 200x90 D=%d paths=%d" % (D, paths))
     assert p.stdout.strip().endswith("GOLDEN OK")
+
+
+HARNESS_LINE = re.compile(
+    r"^gb300\s+(\d+)x(\d+) D=(\d+) paths=(\d+) th=(\d+)  median\s+([0-9.]+) ms  p95\s+([0-9.]+)  min\s+([0-9.]+)"
+    r"  sd\s+([0-9.]+)  spread ([0-9.]+)/([0-9.]+)( UNSTABLE)?  fps\s+([0-9.]+)  Mpix/s\s+([0-9.]+)  hash ([0-9a-f]{16})"
+    r"(  GOLDEN OK|  GOLDEN FAIL)?$")
+HARNESS_JSON_KEYS = {"impl", "board", "W", "H", "D", "paths", "census", "P1", "P2", "threads", "threads_requested",
+                     "cpu_mask", "warm", "timed", "median_ms", "p95_ms", "min_ms", "rmsd_ms", "spread_hi", "spread_lo",
+                     "unstable", "transfer_ms", "threads_used", "fps", "mpix_s", "census_ms", "cost_ms",
+                     "aggregate_ms", "argmin_ms", "hash", "golden_match", "roofline_ok", "cflags", "git", "ts"}
+
+
+@pytest.mark.gpu
+def test_cli_plain_harness_line_and_record(tmp_path):
+    """`plain` prints the reference harness's result line (common/harness.c:
+    197-201) and appends its JSON record (:207-224) with the same fields."""
+    l, r, _ = sgmgb.synth_pair(320, 200, 64, 4)
+    write_pgm(str(tmp_path / "l.pgm"), l)
+    write_pgm(str(tmp_path / "r.pgm"), r)
+    want = oracle.plain(l, r, 64, 4)
+    write_pgm(str(tmp_path / "g.pgm"), want)
+    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-g", tmp_path / "g.pgm", "-w", 2, "-n", 9, "-t", 4,
+            "-j", tmp_path / "res.jsonl", "--no-roofline")
+    assert p.returncode == 0, p.stdout + p.stderr
+    m = HARNESS_LINE.match(p.stdout.splitlines()[0])
+    assert m, p.stdout
+    assert m.group(1, 2, 3, 4, 5) == ("320", "200", "64", "4", "0")
+    med, p95, mn = float(m.group(6)), float(m.group(7)), float(m.group(8))
+    assert mn <= med <= p95
+    assert m.group(15) == oracle.fnv1a64(want) and m.group(16) == "  GOLDEN OK"
+    rec = json.loads(open(tmp_path / "res.jsonl").read().splitlines()[-1])
+    assert set(rec) == HARNESS_JSON_KEYS
+    assert rec["timed"] == 9 and rec["warm"] == 2 and rec["threads_requested"] == 4 and rec["threads_used"] == 0
+    assert rec["golden_match"] == 1 and rec["roofline_ok"] == -1 and rec["hash"] == oracle.fnv1a64(want)
+    assert rec["aggregate_ms"] >= 0 and rec["cost_ms"] == -1 and rec["argmin_ms"] == -1
+
+
+@pytest.mark.gpu
+def test_cli_plain_cost_gate(tmp_path):
+    """The per-phase cost gate of common/roofline.h: --roofline-calibrate
+    writes gb300 rows; the next run arms against them and passes; a planted
+    calibration 100x cheaper than the engine fails the run with exit 3 while
+    the map stays golden."""
+    l, r, _ = sgmgb.synth_pair(320, 200, 64, 6)
+    write_pgm(str(tmp_path / "l.pgm"), l)
+    write_pgm(str(tmp_path / "r.pgm"), r)
+    cal = tmp_path / "roofline.cal"
+    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-n", 5, "--board", "testbox", "--roofline-calibrate",
+            "--roofline-cal", cal)
+    assert p.returncode == 0, p.stderr
+    rows = [x.split() for x in open(cal).read().splitlines()]
+    assert {x[4] for x in rows} == {"census", "aggregate"}          # cost and argmin are fused (-1)
+    assert all(x[:4] == ["gb300", "testbox", "320x200", "D64"] and float(x[5]) > 0 for x in rows)
+    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-n", 5, "--board", "testbox", "--roofline-cal", cal,
+            "--roofline-max", 5, "-j", tmp_path / "a.jsonl")
+    assert p.returncode == 0, p.stdout + p.stderr
+    assert "roofline:" in p.stdout and "NOT ARMED" not in p.stderr
+    assert json.loads(open(tmp_path / "a.jsonl").read())["roofline_ok"] == 1
+    planted = tmp_path / "planted.cal"
+    planted.write_text("".join("%s %s %s %s %s %.9f\n" % (*x[:5], float(x[5]) / 100) for x in rows))
+    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-n", 3, "--board", "testbox", "--roofline-cal", planted)
+    assert p.returncode == 3 and "ROOFLINE FAIL" in p.stderr
+    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-n", 3, "--board", "other", "--roofline-cal", cal)
+    assert p.returncode == 0 and "NOT ARMED" in p.stderr              # no row for this board: says so
