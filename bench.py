@@ -223,9 +223,14 @@ def batched_section(eng_cls, sgmgb, torch, np):
                     "drop-in calls copy host buffers in and out"}, checks
 
 
-def served_section(eng_cls, sgmgb, np, rate=2000.0, secs=3.0):
+def served_section(eng_cls, sgmgb, np, rates=(2000.0, 3000.0, 4000.0), secs=3.0):
     """8 virtual cameras (sizes from 640x480 / 1280x720 / 1920x1080, D 64/128,
-    4-path), Poisson arrivals at `rate` frames/s in aggregate, 40 GB budget."""
+    4-path), Poisson arrivals at each offered rate in turn (the first, 2000
+    frames/s, is the configuration's), 40 GB budget. Before each run the
+    cameras' slots are made up front (sgmgb_server_prepare), so no device
+    allocation falls inside the run; results are collected on one thread per
+    camera, so a slow frame of one camera holds no other camera's request
+    buffers. Every result is compared with the same frame run alone."""
     import queue
     rng = np.random.default_rng(0)
     sizes = [(640, 480), (1280, 720), (1920, 1080)]
@@ -237,60 +242,75 @@ def served_section(eng_cls, sgmgb, np, rate=2000.0, secs=3.0):
         want[c] = [e.run_frame(l, r) for l, r in scenes[c]]
         e.close()
     eng = eng_cls(0)
-    srv = sgmgb.Server(eng, hbm_budget_bytes=40 << 30, max_inflight=8)
-    for c, (W, H, Dk, P) in cams.items():
-        srv.add_camera(c, W, H, Dk, P)
-    q = queue.Queue()
-    refused = [0]
 
-    def producer():
-        t_next = time.perf_counter()
-        t_end = t_next + secs
-        i = 0
-        while True:
-            t_next += rng.exponential(1.0 / rate)
-            if t_next > t_end:
-                break
-            gap = t_next - time.perf_counter()
-            if gap > 3e-4:
-                time.sleep(gap - 2e-4)      # sleeping releases the interpreter lock for the collector
-            while time.perf_counter() < t_next:
-                pass
-            c = int(rng.integers(0, 8))
-            try:
-                q.put((srv.submit(c, *scenes[c][i % 2]), c, i % 2))
-            except sgmgb.SgmError:
-                refused[0] += 1
-            i += 1
-        q.put(None)
+    def one_run(rate):
+        srv = sgmgb.Server(eng, hbm_budget_bytes=40 << 30, max_inflight=8)
+        for c, (W, H, Dk, P) in cams.items():
+            srv.add_camera(c, W, H, Dk, P)
+        slots = srv.prepare(4)
+        qs = {c: queue.Queue() for c in cams}
+        refused, bad = [0], [0]
+        prng = np.random.default_rng(int(rate))
 
-    bad = [0]
+        def producer():
+            t_next = time.perf_counter()
+            t_end = t_next + secs
+            i = 0
+            while True:
+                t_next += prng.exponential(1.0 / rate)
+                if t_next > t_end:
+                    break
+                gap = t_next - time.perf_counter()
+                if gap > 3e-4:
+                    time.sleep(gap - 2e-4)      # sleeping releases the interpreter lock for the collectors
+                while time.perf_counter() < t_next:
+                    pass
+                c = int(prng.integers(0, 8))
+                try:
+                    qs[c].put((srv.submit(c, *scenes[c][i % 2]), i % 2))
+                except sgmgb.SgmError:
+                    refused[0] += 1
+                i += 1
+            for q in qs.values():
+                q.put(None)
 
-    def consumer():
-        while True:
-            it = q.get()
-            if it is None:
-                return
-            t, c, k = it
-            o, _ = srv.wait(t, 60000)
-            bad[0] += int(not np.array_equal(o, want[c][k]))
+        def collector(c):
+            while True:
+                it = qs[c].get()
+                if it is None:
+                    return
+                t, k = it
+                o, _ = srv.wait(t, 60000)
+                if not np.array_equal(o, want[c][k]):
+                    bad[0] += 1
 
-    switch = sys.getswitchinterval()
-    sys.setswitchinterval(2e-4)             # the two client threads share the interpreter lock finely
-    th = [threading.Thread(target=producer), threading.Thread(target=consumer)]
-    for t in th:
-        t.start()
-    for t in th:
-        t.join()
-    sys.setswitchinterval(switch)
-    st = srv.stats()
-    srv.close()
+        switch = sys.getswitchinterval()
+        sys.setswitchinterval(2e-4)             # the client threads share the interpreter lock finely
+        th = [threading.Thread(target=producer)] + [threading.Thread(target=collector, args=(c,)) for c in cams]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        sys.setswitchinterval(switch)
+        st = srv.stats()
+        srv.close()
+        return {"offered_fps": rate, "fps": st["fps"], "frames_done": st["frames_done"],
+                "frames_refused": st["frames_refused"], "p50_ms": st["p50_ms"],
+                "p99_ms": st["p99_ms"], "max_ms": st["max_ms"], "resident_gb": st["resident_bytes"] / 1e9,
+                "slots": slots, "results_differing_from_alone": bad[0]}
+
+    runs = [one_run(r) for r in rates]
     eng.close()
-    return {"cameras": {str(c): "%dx%d D=%d" % v[:3] for c, v in cams.items()}, "offered_fps": rate,
-            "seconds": secs, "frames_done": st["frames_done"], "frames_refused": st["frames_refused"],
-            "fps": st["fps"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
-            "resident_gb": st["resident_bytes"] / 1e9, "budget_gb": 40 * 2 ** 30 / 1e9,
-            "results_differing_from_alone": bad[0],
+    base = runs[0]
+    ok = [r for r in runs if r["frames_refused"] == 0 and r["results_differing_from_alone"] == 0]
+    return {"cameras": {str(c): "%dx%d D=%d" % v[:3] for c, v in cams.items()}, "offered_fps": base["offered_fps"],
+            "seconds": secs, "frames_done": base["frames_done"], "frames_refused": base["frames_refused"],
+            "fps": base["fps"], "p50_ms": base["p50_ms"], "p99_ms": base["p99_ms"], "max_ms": base["max_ms"],
+            "resident_gb": base["resident_gb"], "slots": base["slots"], "budget_gb": 40 * 2 ** 30 / 1e9,
+            "results_differing_from_alone": sum(r["results_differing_from_alone"] for r in runs),
+            "load_sweep": runs,
+            "capacity_fps": max(r["fps"] for r in ok) if ok else None,
+            "capacity_note": "the highest sustained frames/s of the load sweep with no frame refused",
             "latency": "submit (host copy into pinned memory) to result in pinned host memory"}
 
 

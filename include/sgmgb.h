@@ -250,6 +250,12 @@ int  sgmgb_server_create(sgmgb_ctx *ctx, const sgmgb_server_config *cfg,
 /* Registers a camera: allocates its resident buffers if the budget allows
  * (SGMGB_ERR_BUDGET otherwise). */
 int  sgmgb_server_add_camera(sgmgb_server *s, int cam_id, const sgmgb_frame_desc *fd);
+/* Makes every camera's resident slots up front, up to slots_per_camera each
+ * (at most 4), one per camera in turn while the HBM budget allows, so that
+ * no slot is allocated after the first frame is submitted (frames otherwise
+ * grow a camera's slots on demand, and an allocation can stall the device).
+ * *slots_resident (may be NULL) receives the total number of slots. */
+int  sgmgb_server_prepare(sgmgb_server *s, int slots_per_camera, int *slots_resident);
 /* Submits one frame (host buffers of W*H bytes, copied before returning).
  * Admitted frames join the device work immediately; *ticket identifies it.
  * SGMGB_ERR_BUDGET when no slot is free for this camera. */

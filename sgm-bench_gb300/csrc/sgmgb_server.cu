@@ -4,8 +4,10 @@
 // Per camera:
 //   - slots: resident device workspaces (inputs, census, cost, planes, sums,
 //     output) sized for the camera's frame description. The first is allocated
-//     when the camera is added; more are added on demand while the HBM budget
-//     and the in-flight limit allow, and they stay resident.
+//     when the camera is added; sgmgb_server_prepare makes more up front
+//     (round-robin over the cameras, within the HBM budget), and otherwise
+//     they are added on demand while the budget and the in-flight limit
+//     allow. They stay resident.
 //   - request buffers: pinned host memory holding one request's two input
 //     images and its output map. submit() copies the caller's images into a
 //     free one (or refuses the frame when none is free), so the H2D and D2H
@@ -228,8 +230,13 @@ void worker_main(sgmgb_server *s) {
                     continue;
                 }
                 sl.busy = true;
-                c->slots.push_back(sl);          // slots are only touched by this thread
-                a.slot = (int)c->slots.size() - 1;
+                {
+                    // appended under the lock (sgmgb_server_prepare appends too); the
+                    // vector's capacity is reserved, so no slot ever moves
+                    std::lock_guard<std::mutex> g(s->mu);
+                    c->slots.push_back(sl);
+                    a.slot = (int)c->slots.size() - 1;
+                }
                 grown.push_back({c, a.grow});
             }
             a.r->slot = a.slot;
@@ -329,6 +336,7 @@ int sgmgb_server_add_camera(sgmgb_server *s, int cam_id, const sgmgb_frame_desc 
         delete c;
         return serr(s, SGMGB_ERR_NOMEM, "server: camera " + std::to_string(cam_id) + ": slot allocation failed");
     }
+    c->slots.reserve(kMaxSlotsPerCamera);   // slots never move once made
     c->slots.push_back(first);
     for (int i = 0; i < kReqBufsPerCamera; i++) {
         uint8_t *p = nullptr;
@@ -351,6 +359,46 @@ int sgmgb_server_add_camera(sgmgb_server *s, int cam_id, const sgmgb_frame_desc 
     std::lock_guard<std::mutex> g(s->mu);
     s->adding.erase(cam_id);
     s->cams[cam_id] = c;
+    return SGMGB_OK;
+}
+
+int sgmgb_server_prepare(sgmgb_server *s, int slots_per_camera, int *slots_resident) {
+    if (!s || slots_per_camera < 1) return SGMGB_ERR_ARG;
+    const int want = std::min(slots_per_camera, kMaxSlotsPerCamera);
+    cudaSetDevice(s->ctx->device);
+    // round-robin over the cameras, one slot at a time, so the budget is shared
+    for (bool progress = true; progress;) {
+        progress = false;
+        std::vector<std::pair<Camera *, size_t>> todo;
+        {
+            std::lock_guard<std::mutex> g(s->mu);
+            for (auto &kv : s->cams) {
+                Camera *c = kv.second;
+                if ((int)c->slots.size() + c->growing >= want) continue;
+                const size_t need = growth_bytes(s, c);
+                if (!need) continue;
+                c->growing++;
+                s->resident += need;
+                todo.push_back({c, need});
+            }
+        }
+        for (auto &t : todo) {
+            Slot sl;
+            const bool ok = make_slot(t.first->fd, &sl);
+            std::lock_guard<std::mutex> g(s->mu);
+            t.first->growing--;
+            if (!ok) { s->resident -= t.second; continue; }
+            // slots are appended only under the lock while the dispatcher may read them
+            t.first->slots.push_back(sl);
+            progress = true;
+        }
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    if (slots_resident) {
+        int n = 0;
+        for (auto &kv : s->cams) n += (int)kv.second->slots.size();
+        *slots_resident = n;
+    }
     return SGMGB_OK;
 }
 

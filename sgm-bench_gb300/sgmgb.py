@@ -34,6 +34,7 @@ EXPORTS = [
     "sgmgb_batch_destroy", "sgmgb_tune_lookup", "sgmgb_tune_record",
     "sgmgb_server_create", "sgmgb_server_add_camera", "sgmgb_server_submit", "sgmgb_server_poll",
     "sgmgb_server_wait", "sgmgb_server_stats_get", "sgmgb_server_destroy", "sgmgb_synth_pair",
+    "sgmgb_server_prepare",
     "sgmgb_run_frame_noalloc",
 ]
 
@@ -108,6 +109,7 @@ def _load():
         "sgmgb_tune_record": (i, [ctypes.c_char_p, fdp, i, i, ctypes.c_double]),
         "sgmgb_server_create": (i, [vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]),
         "sgmgb_server_add_camera": (i, [vp, i, fdp]),
+        "sgmgb_server_prepare": (i, [vp, i, ctypes.POINTER(i)]),
         "sgmgb_server_submit": (i, [vp, i, u8p, u8p, ctypes.POINTER(ctypes.c_uint64)]),
         "sgmgb_server_poll": (i, [vp, ctypes.c_uint64, u8p, ctypes.POINTER(ctypes.c_double)]),
         "sgmgb_server_wait": (i, [vp, ctypes.c_uint64, u8p, ctypes.POINTER(ctypes.c_double), i]),
@@ -350,6 +352,13 @@ class Server:
         fd = desc(W, H, D, paths, variant)
         self.engine._check(lib.sgmgb_server_add_camera(self.h, cam_id, ctypes.byref(fd)))
         self.cams[cam_id] = fd
+
+    def prepare(self, slots_per_camera=4):
+        """Makes the cameras' slots up front (round-robin, within the budget);
+        returns the number of resident slots."""
+        n = ctypes.c_int()
+        self.engine._check(lib.sgmgb_server_prepare(self.h, slots_per_camera, ctypes.byref(n)))
+        return n.value
 
     def submit(self, cam_id, left, right):
         left = np.ascontiguousarray(left, np.uint8)

@@ -105,3 +105,25 @@ def test_server_refuses_when_request_buffers_run_out(engine):
     with pytest.raises(sgmgb.SgmError):
         s.submit(99, l, r)                         # unknown camera
     s.close()
+
+
+def test_server_prepare_makes_slots_up_front_within_budget(engine):
+    """sgmgb_server_prepare makes each camera's slots before any frame (up to
+    4 per camera, one camera at a time while the budget allows), and frames
+    submitted afterwards allocate nothing more: the resident bytes stay put."""
+    one = sgmgb.workspace_bytes(160, 96, 64, 4)
+    s = sgmgb.Server(engine, hbm_budget_bytes=5 * one, max_inflight=8)
+    s.add_camera(0, 160, 96, 64, 4)
+    s.add_camera(1, 160, 96, 64, 4)
+    assert s.stats()["resident_bytes"] == 2 * one
+    assert s.prepare(4) == 5                       # 2 + 3 more before the budget stops it, shared in turn
+    assert s.stats()["resident_bytes"] == 5 * one
+    assert s.prepare(4) == 5                       # nothing left to make
+    frames = [(cam, *sgmgb.synth_pair(160, 96, 64, seed=20 + k)[:2]) for k in range(6) for cam in (0, 1)]
+    tickets = [s.submit(cam, l, r) for cam, l, r in frames]
+    for (cam, l, r), t in zip(frames, tickets):
+        assert np.array_equal(s.wait(t)[0], oracle.plain(l, r, 64, 4))
+    assert s.stats()["resident_bytes"] == 5 * one
+    with pytest.raises(sgmgb.SgmError):
+        s.prepare(0)
+    s.close()
