@@ -104,6 +104,12 @@ int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane
  *   THROUGHPUT  the last direction (T->B) adds the other directions' planes
  *               to its own L and takes the argmin: one plane less written and
  *               read per frame, for frames that share the GPU;
+ *   FUSED       the two horizontal directions split each row in halves: the
+ *               first halves compute the matching costs themselves (no cost
+ *               pass) and park L; the vertical directions park theirs; the
+ *               second halves resume the rows, add the three planes and take
+ *               the argmin. Plain variant, 4 paths, D = 32, 64 or 128 in the
+ *               default path shape; other frames run THROUGHPUT;
  *   AUTO        LATENCY for sgmgb_run_frame and for a server frame with
  *               nothing else in flight, THROUGHPUT for sgmgb_run_frame_async
  *               and the other server frames (the default).
@@ -111,6 +117,7 @@ int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane
 #define SGMGB_SCHED_AUTO       0
 #define SGMGB_SCHED_LATENCY    1
 #define SGMGB_SCHED_THROUGHPUT 2
+#define SGMGB_SCHED_FUSED      3
 int  sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule);
 
 /* ---- single frame ---- */

@@ -24,6 +24,13 @@ inline PathShape resolve_sched(PathShape s, bool alone) {
     return s;
 }
 
+// The fused schedule covers the plain variant with 4 paths in the
+// two-lines-per-warp layout (D = 32, 64 or 128, no disparities-per-lane
+// shape); other frames asking for it run the throughput schedule.
+inline bool fused_applies(const sgmgb_frame_desc &fd, const PathShape &s) {
+    return fd.variant == SGMGB_PLAIN && fd.paths == 4 && s.dpl == 0 && (fd.D == 32 || fd.D == 64 || fd.D == 128);
+}
+
 struct sgmgb_ctx {
     int device = 0;
     int sm_count = 0;
@@ -57,6 +64,7 @@ struct FrameSlot {
     uint8_t *sc = nullptr;                                        // W*H*D scratch L
     uint16_t *S = nullptr;                                        // W*H*D sum (or two u8 planes)
     uint8_t *xp = nullptr;                                        // 1 (4 paths) or 5 (8 paths) more W*H*D u8 planes
+    uint32_t *state = nullptr;                                    // line state of split rows (fused schedule)
     // multi-scale extras
     uint8_t *sobL = nullptr, *sobR = nullptr;                     // full-scale SobelX
     uint8_t *halfL = nullptr, *halfR = nullptr;                   // half-scale images

@@ -40,6 +40,12 @@ struct LineParams {
                                  // the map (W/2)x(H/2)
     int key16;                   // final: S*64 + d fits 16 bits (4 paths, D <= 64)
     int dpl;                     // disparities per lane: 2, 4 or 8; 0 picks the smallest valid
+    // split horizontal lines (the fused schedule): hseg 1 walks the first half
+    // of each row (L->R x in [0, W/2), R->L x in [W/2, W)), hseg 2 the second
+    // half (L->R [W/2, W), R->L [0, W/2)); 0 the whole line.
+    int hseg;
+    const uint64_t *cl, *cr;     // census descriptors (the first-half pass computes its costs from them)
+    uint32_t *state;             // per warp and lane: L and min at the end of the first half
 };
 
 // Disparities per lane of the path kernel: `want` (0, 2, 4 or 8) raised to
@@ -67,6 +73,11 @@ inline int lines_for_even(int W, int H, int dx, int dy) {
     const int n2 = W - 1 >= m0 ? (W - 1 - m0) / 2 + 1 : 0;
     return n1 + n2;
 }
+
+// Words of line state the first half of a split horizontal pass leaves for
+// the second half: per direction, row pair and lane, the NR packed L
+// registers and the packed minimum (NR = D/32, at most 4).
+inline size_t hstate_words(int H) { return (size_t)2 * ((H + 1) / 2) * 32 * 5; }
 
 // ---- launchers (all enqueue on `s`, none synchronises) ----
 cudaError_t launch_census2(const uint8_t *im0, const uint8_t *im1, uint64_t *out0, uint64_t *out1,
@@ -97,6 +108,14 @@ inline cudaError_t set_carveout(K *kernel) {
 // One direction's path pass over the cost volume p.C (sgmgb_path.cu).
 // saturate: clamp L to 255 (multi-scale). warps_per_block in 1..4.
 cudaError_t launch_line(const LineParams &p, int mode, int saturate, int warps_per_block, cudaStream_t s);
+
+// The first half of both horizontal passes of the fused schedule
+// (sgmgb_fused.cu): per row pair and direction, the Hamming costs of the half
+// row from p.cl / p.cr (stored into p.C), the recurrence (L into the plane
+// p.sc) and the line state at the half's end into p.state. D = 32, 64 or 128,
+// plain variant. warps_per_block in 1..4.
+cudaError_t launch_hcost(const LineParams &p, int warps_per_block, cudaStream_t s);
+cudaError_t prepare_fused_kernels();
 
 // Planes of one frame's directions, each W*H*D uint8 in the cost volume's
 // layout (16-byte aligned).

@@ -219,6 +219,12 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
 #pragma unroll
     for (int j = 0; j < NR; j++) L[j] = 0u;
     uint32_t mn = 0;                                  // L_prev = 0, min_prev = 0: the first step yields L = C
+    if (P.state) {                                    // second half of a split row: resume the first half's line
+        const uint32_t *st = P.state + ((size_t)((P.dx > 0 ? 0 : 1) * ((P.nlines + 1) >> 1) + warp) * 32 + lane) * (NR + 1);
+#pragma unroll
+        for (int j = 0; j < NR; j++) L[j] = st[j];
+        mn = st[NR];
+    }
     uint32_t dpk[NR];                                 // (d, d) for the argmin keys
 #pragma unroll
     for (int j = 0; j < NR; j++) dpk[j] = pk2((uint32_t)(lane * NR + j));

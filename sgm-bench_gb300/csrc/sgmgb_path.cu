@@ -113,6 +113,7 @@ static cudaError_t prep_dpl() {
 cudaError_t prepare_path_kernels() {
     cudaError_t e;
     if ((e = prepare_frame_kernels()) != cudaSuccess) return e;
+    if ((e = prepare_fused_kernels()) != cudaSuccess) return e;
     if ((e = prep_pair_modes<1, 0>()) != cudaSuccess) return e;
     if ((e = prep_pair_modes<2, 0>()) != cudaSuccess) return e;
     if ((e = prep_pair_modes<4, 0>()) != cudaSuccess) return e;

@@ -65,7 +65,15 @@ __device__ __forceinline__ void line_start(const LineParams &P, int line, int &x
             else l = P.H - 1 + (((xe + ye) & 1) ? 1 : 2) + 2 * (line - n1);   // entry column xe + dx*(l-H+1)
         }
     }
-    if (dy == 0) { x = xe; y = l; len = P.W; }
+    if (dy == 0) {
+        x = xe; y = l; len = P.W;
+        if (P.hseg) {                                  // half of the row (split horizontal lines)
+            const int m = P.W >> 1;
+            const bool first = P.hseg == 1;
+            if (dx > 0) { x = first ? 0 : m; len = first ? m : P.W - m; }
+            else { x = first ? P.W - 1 : m - 1; len = first ? P.W - m : m; }
+        }
+    }
     else if (dx == 0) { x = l; y = ye; len = P.H; }
     else {
         if (l < P.H) { x = xe; y = l; }

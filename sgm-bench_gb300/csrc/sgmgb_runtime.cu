@@ -28,6 +28,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
     const size_t o_cl = take(N * 8), o_cr = take(N * 8);
     const size_t o_C = take(N * D), o_sc = take(N * D), o_S = take(N * D * 2);
     const size_t o_xp = take(N * D * (fd.paths == 8 ? 5 : 1));
+    const size_t o_state = fd.variant == SGMGB_PLAIN ? take(hstate_words(fd.H) * 4) : 0;
     size_t o_sobL = 0, o_sobR = 0, o_hL = 0, o_hR = 0, o_hsL = 0, o_hsR = 0, o_cl1 = 0, o_cr1 = 0, o_d1 = 0;
     size_t o_C1 = 0;
     if (fd.variant == SGMGB_MULTISCALE) {
@@ -44,6 +45,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
         s->cl = (uint64_t *)(b + o_cl); s->cr = (uint64_t *)(b + o_cr);
         s->C = b + o_C; s->sc = b + o_sc; s->S = (uint16_t *)(b + o_S);
         s->xp = b + o_xp;
+        s->state = fd.variant == SGMGB_PLAIN ? (uint32_t *)(b + o_state) : nullptr;
         if (fd.variant == SGMGB_MULTISCALE) {
             s->C1 = b + o_C1;
             s->sobL = b + o_sobL; s->sobR = b + o_sobR;
@@ -219,6 +221,60 @@ cudaError_t run_planes(const FrameSlot &s, const LineParams &base, int npaths, i
     return mark("sum_argmin", npaths * Nsum * base.D + Nout);
 }
 
+// The FUSED schedule (plain, 4 paths, pair layout; fused_applies), after the
+// census: the first halves of both horizontal passes compute the costs from
+// the census descriptors into the cost volume and park their L in one plane
+// (the two halves are disjoint columns); the vertical passes, side by side,
+// park theirs in two more; the second halves of the horizontal passes, side
+// by side, resume each row from the first halves' state, add the three
+// planes to their own L and take the argmin. One cost pass fewer than the
+// other schedules, and its population counts run inside the latency-bound
+// horizontal pass; the frame's critical path is census, the first halves,
+// the vertical passes and the second halves.
+cudaError_t run_fused(const FrameSlot &s, const LineParams &base, int wpb, cudaStream_t st, Marker &mark,
+                      uint8_t *disp, double N) {
+    const bool serial = mark.pr != nullptr;
+    const size_t plane = (size_t)base.W * base.H * base.D;
+    const double ND = (double)plane;
+    uint8_t *ph = s.sc, *ptb = (uint8_t *)s.S, *pbt = (uint8_t *)s.S + plane;
+    cudaError_t e;
+    LineParams q = base;
+    q.cl = s.cl; q.cr = s.cr; q.sc = ph; q.state = s.state; q.hseg = 1;
+    if ((e = launch_hcost(q, wpb, st)) != cudaSuccess) return e;
+    if ((e = mark("path_h_first_cost", 16 * N + 2 * ND)) != cudaSuccess) return e;
+    // two independent passes side by side (one after the other with a probe)
+    auto pair_of = [&](const LineParams &a, const LineParams &b, int mode, const char *na, const char *nb,
+                       double bytes) -> cudaError_t {
+        cudaStream_t s2 = serial ? st : s.aux[0];
+        cudaError_t r;
+        if (!serial) {
+            if ((r = cudaEventRecord(s.fork, st)) != cudaSuccess) return r;
+            if ((r = cudaStreamWaitEvent(s2, s.fork, 0)) != cudaSuccess) return r;
+        }
+        if ((r = launch_line(a, mode, 0, wpb, st)) != cudaSuccess) return r;
+        if ((r = mark(na, bytes)) != cudaSuccess) return r;
+        if ((r = launch_line(b, mode, 0, wpb, s2)) != cudaSuccess) return r;
+        if ((r = mark(nb, bytes)) != cudaSuccess) return r;
+        if (!serial) {
+            if ((r = cudaEventRecord(s.join[0], s2)) != cudaSuccess) return r;
+            if ((r = cudaStreamWaitEvent(st, s.join[0], 0)) != cudaSuccess) return r;
+        }
+        return cudaSuccess;
+    };
+    LineParams tb = base, bt = base;
+    tb.dx = 0; tb.dy = 1; tb.sc = ptb; tb.nlines = lines_for(base.W, base.H, 0, 1);
+    bt.dx = 0; bt.dy = -1; bt.sc = pbt; bt.nlines = tb.nlines;
+    if ((e = pair_of(tb, bt, MODE_SCRATCH, "path_tb", "path_bt", 2 * ND)) != cudaSuccess) return e;
+    LineParams lr = base;
+    lr.dx = 1; lr.dy = 0; lr.hseg = 2; lr.state = s.state;
+    lr.sc = ph; lr.sc2 = ptb; lr.sc3 = pbt; lr.disp = disp;
+    lr.nlines = lines_for(base.W, base.H, 1, 0);
+    lr.key16 = base.D <= 64 ? 1 : 0;                      // S*64 + d < 2^16 with 4 paths
+    LineParams rl = lr;
+    rl.dx = -1;
+    return pair_of(lr, rl, MODE_FINAL3, "path_lr_final", "path_rl_final", 2 * ND + N / 2);
+}
+
 cudaError_t run_dirs(const PathShape &shape, const FrameSlot &s, const LineParams &base, int npaths, int sat,
                      bool ms, cudaStream_t st, Marker &mark, int even_only, uint8_t *disp, double Nout) {
     if (shape.sched == SGMGB_SCHED_LATENCY)
@@ -236,7 +292,14 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
     const double N = (double)fd.W * fd.H, ND = N * fd.D;
     cudaError_t e;
     if ((e = mark.start()) != cudaSuccess) return e;
-    if (fd.variant == SGMGB_PLAIN) {
+    if (fd.variant == SGMGB_PLAIN && shape.sched == SGMGB_SCHED_FUSED && fused_applies(fd, shape)) {
+        if ((e = launch_census2(d_left, d_right, s.cl, s.cr, fd.W, fd.H, st)) != cudaSuccess) return e;
+        if ((e = mark("census", 18 * N)) != cudaSuccess) return e;
+        if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
+        LineParams p{};
+        p.C = s.C; p.W = fd.W; p.H = fd.H; p.D = fd.D; p.dpl = 0; p.p1 = 20; p.p2 = 192;
+        if ((e = run_fused(s, p, shape.wpb, st, mark, d_disp, N)) != cudaSuccess) return e;
+    } else if (fd.variant == SGMGB_PLAIN) {
         if ((e = launch_census2(d_left, d_right, s.cl, s.cr, fd.W, fd.H, st)) != cudaSuccess) return e;
         if ((e = mark("census", 18 * N)) != cudaSuccess) return e;
         if ((e = launch_cost(s.cl, s.cr, s.C, nullptr, fd.W, fd.H, fd.D, kInvalidPlain, st)) != cudaSuccess)
@@ -416,8 +479,9 @@ int sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane)
 
 int sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule) {
     if (!ctx) return SGMGB_ERR_ARG;
-    if (schedule != SGMGB_SCHED_AUTO && schedule != SGMGB_SCHED_LATENCY && schedule != SGMGB_SCHED_THROUGHPUT)
-        return set_err(ctx, SGMGB_ERR_ARG, "schedule must be SGMGB_SCHED_AUTO, _LATENCY or _THROUGHPUT");
+    if (schedule != SGMGB_SCHED_AUTO && schedule != SGMGB_SCHED_LATENCY && schedule != SGMGB_SCHED_THROUGHPUT &&
+        schedule != SGMGB_SCHED_FUSED)
+        return set_err(ctx, SGMGB_ERR_ARG, "schedule must be SGMGB_SCHED_AUTO, _LATENCY, _THROUGHPUT or _FUSED");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     drop_graph(ctx);
@@ -461,9 +525,10 @@ int sgmgb_plan(sgmgb_ctx *ctx, const sgmgb_frame_desc *fd) {
     const size_t N = (size_t)fd->W * fd->H;
     cudaError_t e = cudaMemsetAsync(s.left, 0, N, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.right, 0, N, ctx->stream);
-    for (int sched : {SGMGB_SCHED_LATENCY, SGMGB_SCHED_THROUGHPUT}) {
+    for (int sched : {SGMGB_SCHED_LATENCY, SGMGB_SCHED_THROUGHPUT, SGMGB_SCHED_FUSED}) {
         PathShape sh = ctx->shape;
         sh.sched = sched;
+        if (sched == SGMGB_SCHED_FUSED && !fused_applies(*fd, sh)) continue;
         if (e == cudaSuccess) e = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, sh, nullptr, nullptr);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);

@@ -112,10 +112,12 @@ def test_cli_plain_golden(tmp_path, D, paths):
     write_pgm(str(tmp_path / "r.pgm"), r)
     want = oracle.plain(l, r, D, paths)
     write_pgm(str(tmp_path / "g.pgm"), want)
-    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-D", D, "-p", paths, "-g", tmp_path / "g.pgm", "-n", 2)
+    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-D", D, "-p", paths, "-g", tmp_path / "g.pgm", "-n", 2,
+            "--no-roofline")
     assert p.returncode == 0, p.stdout + p.stderr
-    assert p.stdout.startswith("gb300  in 200x90 D=%d paths=%d" % (D, paths))
-    assert p.stdout.strip().endswith("GOLDEN OK")
+    m = HARNESS_LINE.match(p.stdout.splitlines()[0])
+    assert m and m.group(1, 2, 3, 4) == ("200", "90", str(D), str(paths)), p.stdout
+    assert m.group(16) == "  GOLDEN OK"
 
 
 HARNESS_LINE = re.compile(

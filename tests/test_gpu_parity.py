@@ -204,9 +204,11 @@ def test_profile_frame_lists_every_kernel(engine):
     want = oracle.plain(left, right, 64, 4)
     want_ms = oracle.multiscale(left, right)
     dirs4 = ["census", "cost", "path_rl", "path_lr", "path_bt"]
+    fused = ["census", "path_h_first_cost", "path_tb", "path_bt", "path_lr_final", "path_rl_final"]
     cases = [(sgmgb.SCHED_AUTO, dirs4 + ["path_tb", "sum_argmin"], 9),       # a synchronous call: latency
              (sgmgb.SCHED_LATENCY, dirs4 + ["path_tb", "sum_argmin"], 9),
-             (sgmgb.SCHED_THROUGHPUT, dirs4 + ["path_tb_final"], 8)]
+             (sgmgb.SCHED_THROUGHPUT, dirs4 + ["path_tb_final"], 8),
+             (sgmgb.SCHED_FUSED, fused, 8)]                                 # multi-scale: the throughput schedule
     try:
         for sched, names4, per_scale in cases:
             engine.set_schedule(sched)
@@ -215,28 +217,36 @@ def test_profile_frame_lists_every_kernel(engine):
             stats = engine.profile_frame(dl, dr, dd, reps=3)
             assert [s[0] for s in stats] == names4
             assert all(ms > 0 and b > 0 for _, ms, b in stats)
-            assert stats[-1][2] == 4 * W * H * 64 + W * H
+            if sched == sgmgb.SCHED_FUSED:
+                assert sum(b for n, _, b in stats if n.endswith("_final")) == 4 * W * H * 64 + W * H
+            else:
+                assert stats[-1][2] == 4 * W * H * 64 + W * H
             assert np.array_equal(dd.cpu().numpy(), want)   # the timed frames are real frames
             engine.plan(W, H, 64, 8, sgmgb.MULTISCALE)
             dd2 = torch.zeros((H // 2, W // 2), dtype=torch.uint8, device="cuda")
             names = [s[0] for s in engine.profile_frame(dl, dr, dd2, reps=2)]
             assert names[:7] == ["half", "sobel_half", "census_half", "cost_half", "sobel", "census", "cost_merge"]
-            assert len(names) == 7 + 2 * per_scale and names[-1] == names4[-1]
+            assert len(names) == 7 + 2 * per_scale
+            assert names[-1] == (names4[-1] if sched != sgmgb.SCHED_FUSED else "path_tb_final")
             assert np.array_equal(dd2.cpu().numpy(), want_ms)
     finally:
         engine.set_schedule(sgmgb.SCHED_AUTO)
 
 
-@pytest.mark.parametrize("sched", ["latency", "throughput"])
+SCHEDS = {"latency": sgmgb.SCHED_LATENCY, "throughput": sgmgb.SCHED_THROUGHPUT, "fused": sgmgb.SCHED_FUSED}
+
+
+@pytest.mark.parametrize("sched", ["latency", "throughput", "fused"])
 def test_schedules_agree(engine, sched):
     """Both frame schedules, through the host-buffer call and the device-buffer
     call, on the shapes that take the sum pass's other code paths (D/16 not a
     divisor of 32, 32-bit keys, 8 planes, even-only)."""
     import torch
-    engine.set_schedule(sgmgb.SCHED_LATENCY if sched == "latency" else sgmgb.SCHED_THROUGHPUT)
+    engine.set_schedule(SCHEDS[sched])
     try:
         for (W, H, D, paths) in [(300, 70, 48, 4), (301, 71, 128, 4), (160, 90, 32, 8), (200, 64, 64, 8),
-                                 (97, 33, 80, 8)]:
+                                 (97, 33, 80, 8), (301, 71, 64, 4), (130, 9, 32, 4), (1, 5, 64, 4), (3, 1, 128, 4),
+                                 (65, 2, 64, 4), (127, 33, 128, 4)]:
             left, right, _ = sgmgb.synth_pair(W, H, min(D, 128), seed=W + D)
             want = oracle.plain(left, right, D, paths)
             engine.plan(W, H, D, paths)
@@ -255,7 +265,7 @@ def test_schedules_agree(engine, sched):
 
 def test_rejects_bad_schedule(engine):
     with pytest.raises(sgmgb.SgmError):
-        engine.set_schedule(3)
+        engine.set_schedule(4)
     with pytest.raises(sgmgb.SgmError):
         engine.set_schedule(-1)
 
@@ -309,5 +319,32 @@ def test_baseline_size_8path(engine, baseline_frames, sched, frame):
         engine.sync()
         got = dd.cpu().numpy()
         assert np.array_equal(got, want), "async:" + _first_diff(got, want)
+    finally:
+        engine.set_schedule(sgmgb.SCHED_AUTO)
+
+
+@pytest.mark.parametrize("frame", [(1920, 1080, 64, 4), (1280, 720, 128, 4), (1920, 1080, 32, 4)])
+def test_fused_schedule_full_size(engine, frame):
+    """The fused schedule (split rows, costs computed in the first halves) at
+    full size, through the host-buffer and the device-buffer calls, against
+    the checker and against the other schedules' device maps."""
+    import torch
+    from conftest import reference_plain
+    W, H, D, paths = frame
+    left, right, _ = sgmgb.synth_pair(W, H, D, seed=W + D + 7)
+    want = reference_plain(left, right, D, paths)
+    engine.plan(W, H, D, paths)
+    try:
+        for sched in (sgmgb.SCHED_FUSED, sgmgb.SCHED_THROUGHPUT):
+            engine.set_schedule(sched)
+            got = engine.run_frame(left, right)
+            assert np.array_equal(got, want), ("host", sched) + (_first_diff(got, want),)
+            dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
+            dd = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+            for _ in range(2):                                  # graph capture, then replay
+                engine.run_frame_async(dl, dr, dd)
+            engine.sync()
+            got = dd.cpu().numpy()
+            assert np.array_equal(got, want), ("async", sched) + (_first_diff(got, want),)
     finally:
         engine.set_schedule(sgmgb.SCHED_AUTO)
