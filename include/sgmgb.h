@@ -110,6 +110,10 @@ int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane
  *               second halves resume the rows, add the three planes and take
  *               the argmin. Plain variant, 4 paths, D = 32, 64 or 128 in the
  *               default path shape; other frames run THROUGHPUT;
+ *   SPLIT       as FUSED, but the costs come from the cost pass and the
+ *               first halves of the rows run side by side with the vertical
+ *               directions: the shortest critical path of the four. Same
+ *               frames as FUSED; other frames run THROUGHPUT;
  *   AUTO        LATENCY for sgmgb_run_frame and for a server frame with
  *               nothing else in flight, THROUGHPUT for sgmgb_run_frame_async
  *               and the other server frames (the default).
@@ -118,6 +122,7 @@ int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane
 #define SGMGB_SCHED_LATENCY    1
 #define SGMGB_SCHED_THROUGHPUT 2
 #define SGMGB_SCHED_FUSED      3
+#define SGMGB_SCHED_SPLIT      4
 int  sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule);
 
 /* ---- single frame ---- */

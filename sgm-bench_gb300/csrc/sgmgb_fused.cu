@@ -113,29 +113,42 @@ __device__ __forceinline__ void path_hcost(const LineParams &P, int pair, uint64
     long long offa = ((long long)ya * W + x0) * D + lane * NR;   // this lane's bytes of pixel (x, ya)
     long long offb = ((long long)yb * W + x0) * D + lane * NR;
 
-    // one step of both rows at x; VALID: every x - d of the step is >= 0
-    auto step_once = [&](const uint64_t *clc, int k, int x, bool live, auto valid_t) {
+    // The chunk's costs first, all K steps at once (they do not depend on the
+    // recurrence, so their loads and population counts leave its per-step
+    // dependency chain), then the K steps of the recurrence. cc[k][j]: packed
+    // (row a, row b) cost of disparity NR*lane + j at the chunk's step k.
+    // VALID: every x - d of the chunk is >= 0.
+    uint32_t cc[K][NR];
+    auto costs = [&](const uint64_t *clc, int xc, int n, uint8_t *cpa, uint8_t *cpb, auto valid_t) {
         constexpr bool VALID = decltype(valid_t)::value;
-        if (!live) return;                                       // past the half's end (warp-uniform): the state stays
-        if (DX > 0) {
 #pragma unroll
-            for (int j = NR - 1; j > 0; j--) { ca[j] = ca[j - 1]; cb[j] = cb[j - 1]; }
-            const int p = win_pos<NR, CAP>(x - NR * lane);
-            ca[0] = wa[p]; cb[0] = wb[p];
-        } else {
+        for (int k = 0; k < K; k++) {
+            if (!VALID && k >= n) break;                         // past the half's end (warp-uniform)
+            const int x = xc + DX * k;
+            if (DX > 0) {
 #pragma unroll
-            for (int j = 0; j < NR - 1; j++) { ca[j] = ca[j + 1]; cb[j] = cb[j + 1]; }
-            const int p = win_pos<NR, CAP>(x - NR * lane - (NR - 1));
-            ca[NR - 1] = wa[p]; cb[NR - 1] = wb[p];
+                for (int j = NR - 1; j > 0; j--) { ca[j] = ca[j - 1]; cb[j] = cb[j - 1]; }
+                const int p = win_pos<NR, CAP>(x - NR * lane);
+                ca[0] = wa[p]; cb[0] = wb[p];
+            } else {
+#pragma unroll
+                for (int j = 0; j < NR - 1; j++) { ca[j] = ca[j + 1]; cb[j] = cb[j + 1]; }
+                const int p = win_pos<NR, CAP>(x - NR * lane - (NR - 1));
+                ca[NR - 1] = wa[p]; cb[NR - 1] = wb[p];
+            }
+            const uint64_t la = clc[k], lb = clc[K + k];
+#pragma unroll
+            for (int j = 0; j < NR; j++) {
+                uint32_t a = (uint32_t)__popcll(la ^ ca[j]), b = (uint32_t)__popcll(lb ^ cb[j]);
+                if (!VALID && x - NR * lane - j < 0) a = b = (uint32_t)kInvalidPlain;
+                cc[k][j] = __byte_perm(a, b, 0x5410);
+            }
+            st_run<NR>(cpa + DX * D * k, pair_pack<NR, false>(cc[k]));
+            if (has_b) st_run<NR>(cpb + DX * D * k, pair_pack<NR, true>(cc[k]));
         }
-        const uint64_t la = clc[k], lb = clc[K + k];
-        uint32_t c[NR];
-#pragma unroll
-        for (int j = 0; j < NR; j++) {
-            uint32_t a = (uint32_t)__popcll(la ^ ca[j]), b = (uint32_t)__popcll(lb ^ cb[j]);
-            if (!VALID && x - NR * lane - j < 0) a = b = (uint32_t)kInvalidPlain;
-            c[j] = __byte_perm(a, b, 0x5410);
-        }
+    };
+    // one step of the recurrence for both rows; lpa / lpb: the chunk's first pixel in the plane
+    auto step_once = [&](int k, uint8_t *lpa, uint8_t *lpb) {
         const uint32_t up = __shfl_up_sync(kFull, L[NR - 1], 1) | mlo;
         const uint32_t dn = __shfl_down_sync(kFull, L[0], 1) | mhi;
         uint32_t w[NR];
@@ -150,21 +163,15 @@ __device__ __forceinline__ void path_hcost(const LineParams &P, int pair, uint64
         uint32_t tm = kFull;
 #pragma unroll
         for (int j = 0; j < NR; j++) {
-            const uint32_t v = vmin2(w[j], E) + c[j] - mn;
+            const uint32_t v = vmin2(w[j], E) + cc[k][j] - mn;
             L[j] = v;
             tm = vmin2(tm, v);
         }
         const uint32_t ra = __reduce_min_sync(kFull, tm & 0xFFFFu);
         const uint32_t rb = __reduce_min_sync(kFull, tm);
         mn = __byte_perm(ra, rb, 0x7610);
-        st_run<NR>(cost + offa, pair_pack<NR, false>(c));
-        st_run<NR>(P.sc + offa, pair_pack<NR, false>(L));
-        if (has_b) {
-            st_run<NR>(cost + offb, pair_pack<NR, true>(c));
-            st_run<NR>(P.sc + offb, pair_pack<NR, true>(L));
-        }
-        offa += DX * D;
-        offb += DX * D;
+        st_run<NR>(lpa + DX * D * k, pair_pack<NR, false>(L));
+        if (has_b) st_run<NR>(lpb + DX * D * k, pair_pack<NR, true>(L));
     };
 
     for (int ch = 0; ch < nchunks; ch++) {
@@ -185,13 +192,19 @@ __device__ __forceinline__ void path_hcost(const LineParams &P, int pair, uint64
         const uint64_t *clc = clr + (ch % NCH) * 2 * K;
         const int n = min(K, len - s0);
         const int xmin = DX > 0 ? xc : xc - (n - 1);
+        uint8_t *cpa = cost + offa, *cpb = cost + offb, *lpa = P.sc + offa, *lpb = P.sc + offb;
         if (n == K && xmin >= D - 1) {
+            costs(clc, xc, n, cpa, cpb, std::true_type{});
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(clc, k, xc + DX * k, true, std::true_type{});
+            for (int k = 0; k < K; k++) step_once(k, lpa, lpb);
         } else {
+            costs(clc, xc, n, cpa, cpb, std::false_type{});
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(clc, k, xc + DX * k, k < n, std::false_type{});
+            for (int k = 0; k < K; k++)
+                if (k < n) step_once(k, lpa, lpb);               // past the half's end (warp-uniform): the state stays
         }
+        offa += (long long)DX * D * K;
+        offb += (long long)DX * D * K;
     }
     cp_async_wait<0>();                                          // no copy outlives the kernel
     uint32_t *st = P.state + ((size_t)((DX > 0 ? 0 : 1) * npairs + pair) * 32 + lane) * (NR + 1);

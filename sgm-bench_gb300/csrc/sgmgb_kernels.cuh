@@ -19,7 +19,9 @@ enum PassMode : int {
     MODE_ACCUM   = 2,   // S += sc + L
     MODE_FINAL   = 3,   // argmin_d(S + sc + L) -> disp, lowest d on ties
     MODE_FINAL3  = 4,   // argmin_d(sc + sc2 + sc3 + L) -> disp: three other directions' planes
-    MODE_FINAL7  = 5    // argmin_d(L + the seven planes sc, sc2, sc3, xpl[0..3]) -> disp (8 paths)
+    MODE_FINAL7  = 5,   // argmin_d(L + the seven planes sc, sc2, sc3, xpl[0..3]) -> disp (8 paths)
+    MODE_FINAL3H = 6    // MODE_FINAL3 along rows (pair layout only): a chunk's disparities of a row
+                        // are gathered in registers and leave in one store per row and chunk
 };
 
 struct LineParams {

@@ -44,17 +44,18 @@ namespace {
 // frames in flight slower: 0.280 -> 0.292 ms per frame; with three, 0.268 ->
 // 0.261). The other modes keep 512 bytes.
 template <int NR, int MODE> struct PairRing {
-    static constexpr int G = MODE == MODE_SCRATCH ? (NR == 4 ? 4 : 2) : (MODE == MODE_FINAL3 ? 2 : 1);
+    static constexpr bool F3 = MODE == MODE_FINAL3 || MODE == MODE_FINAL3H;
+    static constexpr int G = MODE == MODE_SCRATCH ? (NR == 4 ? 4 : 2) : (F3 ? 2 : 1);
     static constexpr int CB = 512 * G;                             // bytes of one stream per chunk
     static constexpr int K = 8 * G / NR;                           // steps per chunk
-    static constexpr int NCH = MODE == MODE_FINAL3 ? 3 : (NR == 1 ? 4 : (NR == 2 ? 6 : 8));   // ring depth
+    static constexpr int NCH = F3 ? 3 : (NR == 1 ? 4 : (NR == 2 ? 6 : 8));   // ring depth
     static constexpr int SB = 64 * NR;                             // bytes of one stream per step: [A | B]
 };
 // Streams of a chunk slot, in units of CB bytes: the cost bytes, the planes
 // the pass reads (one: sc; three for FINAL3), and the partial sum S (uint16,
 // two units) for ACCUM and FINAL.
 template <int NR, int MODE> struct PairSlot {
-    static constexpr int NPL = MODE == MODE_SCRATCH ? 0 : (MODE == MODE_FINAL3 ? 3 : 1);
+    static constexpr int NPL = MODE == MODE_SCRATCH ? 0 : (PairRing<NR, MODE>::F3 ? 3 : 1);
     static constexpr bool HAS_S = MODE == MODE_ACCUM || MODE == MODE_FINAL;
     static constexpr int U = 1 + NPL + (HAS_S ? 2 : 0);
     static constexpr int BYTES = PairRing<NR, MODE>::CB * U;
@@ -141,7 +142,8 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     constexpr bool HAS_S = PairSlot<NR, MODE>::HAS_S;
     constexpr int SLOT = PairSlot<NR, MODE>::BYTES;
     constexpr int D = 32 * NR;
-    constexpr bool FIN = MODE == MODE_FINAL || MODE == MODE_FINAL3;
+    constexpr bool FIN = MODE == MODE_FINAL || MODE == MODE_FINAL3 || MODE == MODE_FINAL3H;
+    constexpr int KW = (K + 3) / 4;                   // FINAL3H: words of one row's disparities per chunk
     const int lane = threadIdx.x & 31;
     const int la = 2 * warp;
     if (la >= P.nlines) return;                       // whole warp leaves together
@@ -219,11 +221,14 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
 #pragma unroll
     for (int j = 0; j < NR; j++) L[j] = 0u;
     uint32_t mn = 0;                                  // L_prev = 0, min_prev = 0: the first step yields L = C
-    if (P.state) {                                    // second half of a split row: resume the first half's line
-        const uint32_t *st = P.state + ((size_t)((P.dx > 0 ? 0 : 1) * ((P.nlines + 1) >> 1) + warp) * 32 + lane) * (NR + 1);
+    // split rows: the first half (hseg 1) leaves each lane's L and the line
+    // minimum at its end, the second half (hseg 2) resumes from them
+    uint32_t *const hstate = P.state && P.hseg
+        ? P.state + ((size_t)((P.dx > 0 ? 0 : 1) * ((P.nlines + 1) >> 1) + warp) * 32 + lane) * (NR + 1) : nullptr;
+    if (hstate && P.hseg == 2) {
 #pragma unroll
-        for (int j = 0; j < NR; j++) L[j] = st[j];
-        mn = st[NR];
+        for (int j = 0; j < NR; j++) L[j] = hstate[j];
+        mn = hstate[NR];
     }
     uint32_t dpk[NR];                                 // (d, d) for the argmin keys
 #pragma unroll
@@ -231,10 +236,12 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     pa -= step; pb -= step; xa -= dx; ya -= dy; xb -= dx; yb -= dy;
     const int hw = P.W >> 1;
 
-    // one step of both lines; `row`: this step's cost row in the chunk
+    uint32_t dacc[2][KW];                             // FINAL3H: the chunk's disparities of rows A and B, byte k = step k
+    // one step of both lines; `row`: this step's cost row in the chunk; kk: the step within the chunk
     auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&ps)[NR], const uint32_t (&sv)[NR], uint8_t *row,
-                         int i, auto full_t) {
+                         int i, int kk, auto full_t) {
         constexpr bool FULL = decltype(full_t)::value;
+        if (!FULL && i >= maxlen) return;             // past both lines' ends (warp-uniform): L and mn stay
         pa += step; pb += step; xa += dx; ya += dy; xb += dx; yb += dy;
         const uint32_t up = __shfl_up_sync(kFull, L[NR - 1], 1) | mlo;
         const uint32_t dn = __shfl_down_sync(kFull, L[0], 1) | mhi;
@@ -309,6 +316,11 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             da = __reduce_min_sync(kFull, ka) & 0xFFu;
             db = __reduce_min_sync(kFull, kb) & 0xFFu;
         }
+        if (MODE == MODE_FINAL3H) {                   // every lane holds da and db: gather them per chunk
+            dacc[0][kk >> 2] |= da << (8 * (kk & 3));
+            dacc[1][kk >> 2] |= db << (8 * (kk & 3));
+            return;
+        }
         if (lane == 0) {
             if (MODE == MODE_FINAL && P.even_only) {  // multi-scale: the map at (2x, 2y) only
                 if (live_a && !((xa | ya) & 1)) P.disp[(long long)(ya >> 1) * hw + (xa >> 1)] = (uint8_t)da;
@@ -354,12 +366,37 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
                 pair_unpack16<NR>(sa, sb, sv[k]);
             }
         }
+        const long long pa0 = pa + step, pb0 = pb + step;   // the chunk's first pixel of each line
+        if (MODE == MODE_FINAL3H) {
+#pragma unroll
+            for (int w = 0; w < KW; w++) dacc[0][w] = dacc[1][w] = 0u;
+        }
         if ((ch + 1) * K <= minlen) {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, std::true_type{});
+            for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, k, std::true_type{});
         } else {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, std::false_type{});
+            for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, k, std::false_type{});
+        }
+        if (MODE == MODE_FINAL3H && lane == 0) {
+            // row r's live steps of the chunk go to disp[p0 + dx*k]: one word store per 4 steps
+            // when the chunk is whole and its span word-aligned, byte stores otherwise
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int n = min(K, (r ? lenb : lena) - ch * K);
+                if (n <= 0) continue;
+                const long long p0 = r ? pb0 : pa0;
+                const long long lo = dx > 0 ? p0 : p0 - (K - 1);     // lowest address of a whole chunk
+                if (n == K && K % 4 == 0 && (((uintptr_t)(P.disp + lo)) & 3) == 0) {
+#pragma unroll
+                    for (int w = 0; w < KW; w++)
+                        ((uint32_t *)(P.disp + lo))[w] = dx > 0 ? dacc[r][w] : __byte_perm(dacc[r][KW - 1 - w], 0, 0x0123);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < K; k++)
+                        if (k < n) P.disp[p0 + dx * k] = (uint8_t)(dacc[r][k >> 2] >> (8 * (k & 3)));
+                }
+            }
         }
         if (MODE == MODE_SCRATCH) {
             __syncwarp();                             // every lane's L bytes of the chunk are staged
@@ -372,6 +409,11 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         }
     }
     cp_async_wait<0>();                               // no copy outlives the kernel
+    if (hstate && P.hseg == 1) {
+#pragma unroll
+        for (int j = 0; j < NR; j++) hstate[j] = L[j];
+        hstate[NR] = mn;
+    }
 }
 
 }  // namespace sgmgb

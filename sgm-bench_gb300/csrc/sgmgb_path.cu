@@ -58,7 +58,7 @@ static cudaError_t launch_pair_one(const LineParams &p, int wpb, cudaStream_t s)
 static bool pair_applies(const LineParams &p, int mode, int saturate) {
     if (p.dpl != 0 || (p.D != 32 && p.D != 64 && p.D != 128)) return false;
     if (mode == MODE_SCRATCH) return !saturate || p.D == 64;   // the multi-scale passes (saturating, D = 64)
-    return mode == MODE_FINAL3 && !saturate;
+    return (mode == MODE_FINAL3 || mode == MODE_FINAL3H) && !saturate;
 }
 
 template <int NR, int SAT>
@@ -82,6 +82,14 @@ static cudaError_t launch_pair(const LineParams &p, int mode, int saturate, int 
         case 64: return key16 ? launch_pair_one<2, MODE_FINAL3, 0, true>(p, wpb, s)
                               : launch_pair_one<2, MODE_FINAL3, 0, false>(p, wpb, s);
         default: return launch_pair_one<4, MODE_FINAL3, 0, false>(p, wpb, s);
+        }
+    }
+    if (mode == MODE_FINAL3H) {                       // rows only (the fused schedule's second halves)
+        if (p.dy != 0) return cudaErrorInvalidValue;
+        switch (p.D) {
+        case 32: return launch_pair_one<1, MODE_FINAL3H, 0, true>(p, wpb, s);
+        case 64: return launch_pair_one<2, MODE_FINAL3H, 0, true>(p, wpb, s);
+        default: return launch_pair_one<4, MODE_FINAL3H, 0, false>(p, wpb, s);
         }
     }
     switch (p.D) {
@@ -123,6 +131,9 @@ cudaError_t prepare_path_kernels() {
     if ((e = prep_pair<2, MODE_FINAL3, 0, true>()) != cudaSuccess) return e;
     if ((e = prep_pair<2, MODE_FINAL3, 0, false>()) != cudaSuccess) return e;
     if ((e = prep_pair<4, MODE_FINAL3, 0, false>()) != cudaSuccess) return e;
+    if ((e = prep_pair<1, MODE_FINAL3H, 0, true>()) != cudaSuccess) return e;
+    if ((e = prep_pair<2, MODE_FINAL3H, 0, true>()) != cudaSuccess) return e;
+    if ((e = prep_pair<4, MODE_FINAL3H, 0, false>()) != cudaSuccess) return e;
     if ((e = prep_dpl<2, 0, false>()) != cudaSuccess) return e;
     if ((e = prep_dpl<2, 0, true>()) != cudaSuccess) return e;
     if ((e = prep_dpl<4, 0, false>()) != cudaSuccess) return e;

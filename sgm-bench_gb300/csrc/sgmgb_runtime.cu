@@ -272,7 +272,70 @@ cudaError_t run_fused(const FrameSlot &s, const LineParams &base, int wpb, cudaS
     lr.key16 = base.D <= 64 ? 1 : 0;                      // S*64 + d < 2^16 with 4 paths
     LineParams rl = lr;
     rl.dx = -1;
-    return pair_of(lr, rl, MODE_FINAL3, "path_lr_final", "path_rl_final", 2 * ND + N / 2);
+    return pair_of(lr, rl, MODE_FINAL3H, "path_lr_final", "path_rl_final", 2 * ND + N / 2);
+}
+
+// The SPLIT schedule (the frames of fused_applies), after census and cost:
+// the first halves of both horizontal passes (plain scratch passes over half
+// of each row, L into one plane, line state at the half's end) run side by
+// side with the two vertical passes; then the second halves resume the rows,
+// add the three planes and take the argmin, as in the FUSED schedule. The
+// cost pass uses the whole GPU, and the half-rows overlap the vertical
+// passes, so the critical path is census, cost, the longer of the vertical
+// pass and the half row, and a half row.
+cudaError_t run_split(const FrameSlot &s, const LineParams &base, int wpb, cudaStream_t st, Marker &mark,
+                      uint8_t *disp, double N) {
+    const bool serial = mark.pr != nullptr;
+    const size_t plane = (size_t)base.W * base.H * base.D;
+    const double ND = (double)plane;
+    uint8_t *ph = s.sc, *ptb = (uint8_t *)s.S, *pbt = (uint8_t *)s.S + plane;
+    LineParams q[4];
+    for (int k = 0; k < 4; k++) q[k] = base;
+    q[0].dx = 1; q[0].dy = 0; q[0].hseg = 1; q[0].state = s.state; q[0].sc = ph;
+    q[1] = q[0]; q[1].dx = -1;
+    q[0].nlines = q[1].nlines = lines_for(base.W, base.H, 1, 0);
+    q[2].dx = 0; q[2].dy = 1; q[2].sc = ptb; q[2].nlines = lines_for(base.W, base.H, 0, 1);
+    q[3] = q[2]; q[3].dy = -1; q[3].sc = pbt;
+    static const char *names[4] = {"path_lr_first", "path_rl_first", "path_tb", "path_bt"};
+    const double bytes[4] = {ND, ND, 2 * ND, 2 * ND};
+    cudaStream_t ss[4];
+    for (int k = 0; k < 4; k++) ss[k] = (serial || k == 0) ? st : s.aux[k - 1];
+    cudaError_t e;
+    if (!serial) {
+        if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
+        for (int k = 1; k < 4; k++)
+            if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
+    }
+    for (int k : {2, 3, 0, 1}) {                          // the longer vertical passes first
+        if ((e = launch_line(q[k], MODE_SCRATCH, 0, wpb, ss[k])) != cudaSuccess) return e;
+        if ((e = mark(names[k], bytes[k])) != cudaSuccess) return e;
+    }
+    if (!serial) {
+        for (int k = 1; k < 4; k++) {
+            if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
+        }
+    }
+    LineParams lr = base;
+    lr.dx = 1; lr.dy = 0; lr.hseg = 2; lr.state = s.state;
+    lr.sc = ph; lr.sc2 = ptb; lr.sc3 = pbt; lr.disp = disp;
+    lr.nlines = lines_for(base.W, base.H, 1, 0);
+    LineParams rl = lr;
+    rl.dx = -1;
+    cudaStream_t s2 = serial ? st : s.aux[0];
+    if (!serial) {
+        if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(s2, s.fork, 0)) != cudaSuccess) return e;
+    }
+    if ((e = launch_line(lr, MODE_FINAL3H, 0, wpb, st)) != cudaSuccess) return e;
+    if ((e = mark("path_lr_final", 2 * ND + N / 2)) != cudaSuccess) return e;
+    if ((e = launch_line(rl, MODE_FINAL3H, 0, wpb, s2)) != cudaSuccess) return e;
+    if ((e = mark("path_rl_final", 2 * ND + N / 2)) != cudaSuccess) return e;
+    if (!serial) {
+        if ((e = cudaEventRecord(s.join[0], s2)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(st, s.join[0], 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t run_dirs(const PathShape &shape, const FrameSlot &s, const LineParams &base, int npaths, int sat,
@@ -299,6 +362,16 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         LineParams p{};
         p.C = s.C; p.W = fd.W; p.H = fd.H; p.D = fd.D; p.dpl = 0; p.p1 = 20; p.p2 = 192;
         if ((e = run_fused(s, p, shape.wpb, st, mark, d_disp, N)) != cudaSuccess) return e;
+    } else if (fd.variant == SGMGB_PLAIN && shape.sched == SGMGB_SCHED_SPLIT && fused_applies(fd, shape)) {
+        if ((e = launch_census2(d_left, d_right, s.cl, s.cr, fd.W, fd.H, st)) != cudaSuccess) return e;
+        if ((e = mark("census", 18 * N)) != cudaSuccess) return e;
+        if ((e = launch_cost(s.cl, s.cr, s.C, nullptr, fd.W, fd.H, fd.D, kInvalidPlain, st)) != cudaSuccess)
+            return e;
+        if ((e = mark("cost", 16 * N + ND)) != cudaSuccess) return e;
+        if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
+        LineParams p{};
+        p.C = s.C; p.W = fd.W; p.H = fd.H; p.D = fd.D; p.dpl = 0; p.p1 = 20; p.p2 = 192;
+        if ((e = run_split(s, p, shape.wpb, st, mark, d_disp, N)) != cudaSuccess) return e;
     } else if (fd.variant == SGMGB_PLAIN) {
         if ((e = launch_census2(d_left, d_right, s.cl, s.cr, fd.W, fd.H, st)) != cudaSuccess) return e;
         if ((e = mark("census", 18 * N)) != cudaSuccess) return e;
@@ -480,8 +553,8 @@ int sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane)
 int sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule) {
     if (!ctx) return SGMGB_ERR_ARG;
     if (schedule != SGMGB_SCHED_AUTO && schedule != SGMGB_SCHED_LATENCY && schedule != SGMGB_SCHED_THROUGHPUT &&
-        schedule != SGMGB_SCHED_FUSED)
-        return set_err(ctx, SGMGB_ERR_ARG, "schedule must be SGMGB_SCHED_AUTO, _LATENCY, _THROUGHPUT or _FUSED");
+        schedule != SGMGB_SCHED_FUSED && schedule != SGMGB_SCHED_SPLIT)
+        return set_err(ctx, SGMGB_ERR_ARG, "schedule must be SGMGB_SCHED_AUTO, _LATENCY, _THROUGHPUT, _FUSED or _SPLIT");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     drop_graph(ctx);
@@ -525,10 +598,10 @@ int sgmgb_plan(sgmgb_ctx *ctx, const sgmgb_frame_desc *fd) {
     const size_t N = (size_t)fd->W * fd->H;
     cudaError_t e = cudaMemsetAsync(s.left, 0, N, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.right, 0, N, ctx->stream);
-    for (int sched : {SGMGB_SCHED_LATENCY, SGMGB_SCHED_THROUGHPUT, SGMGB_SCHED_FUSED}) {
+    for (int sched : {SGMGB_SCHED_LATENCY, SGMGB_SCHED_THROUGHPUT, SGMGB_SCHED_FUSED, SGMGB_SCHED_SPLIT}) {
         PathShape sh = ctx->shape;
         sh.sched = sched;
-        if (sched == SGMGB_SCHED_FUSED && !fused_applies(*fd, sh)) continue;
+        if ((sched == SGMGB_SCHED_FUSED || sched == SGMGB_SCHED_SPLIT) && !fused_applies(*fd, sh)) continue;
         if (e == cudaSuccess) e = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, sh, nullptr, nullptr);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);

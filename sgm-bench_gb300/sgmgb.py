@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD, "libsgmgb.so")
 
 PLAIN, MULTISCALE = 0, 1
-SCHED_AUTO, SCHED_LATENCY, SCHED_THROUGHPUT, SCHED_FUSED = 0, 1, 2, 3
+SCHED_AUTO, SCHED_LATENCY, SCHED_THROUGHPUT, SCHED_FUSED, SCHED_SPLIT = 0, 1, 2, 3, 4
 OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_NODEV, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 
 # every symbol include/sgmgb.h declares
@@ -239,8 +239,8 @@ class Engine:
         return self
 
     def set_schedule(self, schedule=SCHED_AUTO):
-        """Frame schedule: SCHED_LATENCY, SCHED_THROUGHPUT, SCHED_FUSED or
-        SCHED_AUTO (speed only; results are identical)."""
+        """Frame schedule: SCHED_LATENCY, SCHED_THROUGHPUT, SCHED_FUSED,
+        SCHED_SPLIT or SCHED_AUTO (speed only; results are identical)."""
         self._check(lib.sgmgb_set_schedule(self.h, schedule))
         return self
 

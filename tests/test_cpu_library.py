@@ -42,6 +42,7 @@ def test_header_constants_match_the_binding():
     assert defines["SGMGB_SCHED_LATENCY"] == sgmgb.SCHED_LATENCY
     assert defines["SGMGB_SCHED_THROUGHPUT"] == sgmgb.SCHED_THROUGHPUT
     assert defines["SGMGB_SCHED_FUSED"] == sgmgb.SCHED_FUSED
+    assert defines["SGMGB_SCHED_SPLIT"] == sgmgb.SCHED_SPLIT
     enums = {m.group(1): int(m.group(2)) for m in re.finditer(r"(SGMGB_\w+)\s*=\s*(-?\d+)", src)}
     for name, value in (("SGMGB_OK", sgmgb.OK), ("SGMGB_ERR_ARG", sgmgb.ERR_ARG), ("SGMGB_ERR_NOMEM", sgmgb.ERR_NOMEM),
                         ("SGMGB_ERR_CUDA", sgmgb.ERR_CUDA), ("SGMGB_ERR_NODEV", sgmgb.ERR_NODEV),

@@ -208,7 +208,9 @@ def test_profile_frame_lists_every_kernel(engine):
     cases = [(sgmgb.SCHED_AUTO, dirs4 + ["path_tb", "sum_argmin"], 9),       # a synchronous call: latency
              (sgmgb.SCHED_LATENCY, dirs4 + ["path_tb", "sum_argmin"], 9),
              (sgmgb.SCHED_THROUGHPUT, dirs4 + ["path_tb_final"], 8),
-             (sgmgb.SCHED_FUSED, fused, 8)]                                 # multi-scale: the throughput schedule
+             (sgmgb.SCHED_FUSED, fused, 8),                                 # multi-scale: the throughput schedule
+             (sgmgb.SCHED_SPLIT, ["census", "cost", "path_tb", "path_bt", "path_lr_first", "path_rl_first",
+                                  "path_lr_final", "path_rl_final"], 8)]
     try:
         for sched, names4, per_scale in cases:
             engine.set_schedule(sched)
@@ -217,7 +219,7 @@ def test_profile_frame_lists_every_kernel(engine):
             stats = engine.profile_frame(dl, dr, dd, reps=3)
             assert [s[0] for s in stats] == names4
             assert all(ms > 0 and b > 0 for _, ms, b in stats)
-            if sched == sgmgb.SCHED_FUSED:
+            if sched in (sgmgb.SCHED_FUSED, sgmgb.SCHED_SPLIT):
                 assert sum(b for n, _, b in stats if n.endswith("_final")) == 4 * W * H * 64 + W * H
             else:
                 assert stats[-1][2] == 4 * W * H * 64 + W * H
@@ -227,16 +229,18 @@ def test_profile_frame_lists_every_kernel(engine):
             names = [s[0] for s in engine.profile_frame(dl, dr, dd2, reps=2)]
             assert names[:7] == ["half", "sobel_half", "census_half", "cost_half", "sobel", "census", "cost_merge"]
             assert len(names) == 7 + 2 * per_scale
-            assert names[-1] == (names4[-1] if sched != sgmgb.SCHED_FUSED else "path_tb_final")
+            assert names[-1] == (names4[-1] if sched not in (sgmgb.SCHED_FUSED, sgmgb.SCHED_SPLIT)
+                                 else "path_tb_final")
             assert np.array_equal(dd2.cpu().numpy(), want_ms)
     finally:
         engine.set_schedule(sgmgb.SCHED_AUTO)
 
 
-SCHEDS = {"latency": sgmgb.SCHED_LATENCY, "throughput": sgmgb.SCHED_THROUGHPUT, "fused": sgmgb.SCHED_FUSED}
+SCHEDS = {"latency": sgmgb.SCHED_LATENCY, "throughput": sgmgb.SCHED_THROUGHPUT, "fused": sgmgb.SCHED_FUSED,
+          "split": sgmgb.SCHED_SPLIT}
 
 
-@pytest.mark.parametrize("sched", ["latency", "throughput", "fused"])
+@pytest.mark.parametrize("sched", ["latency", "throughput", "fused", "split"])
 def test_schedules_agree(engine, sched):
     """Both frame schedules, through the host-buffer call and the device-buffer
     call, on the shapes that take the sum pass's other code paths (D/16 not a
@@ -265,7 +269,7 @@ def test_schedules_agree(engine, sched):
 
 def test_rejects_bad_schedule(engine):
     with pytest.raises(sgmgb.SgmError):
-        engine.set_schedule(4)
+        engine.set_schedule(5)
     with pytest.raises(sgmgb.SgmError):
         engine.set_schedule(-1)
 
@@ -325,9 +329,9 @@ def test_baseline_size_8path(engine, baseline_frames, sched, frame):
 
 @pytest.mark.parametrize("frame", [(1920, 1080, 64, 4), (1280, 720, 128, 4), (1920, 1080, 32, 4)])
 def test_fused_schedule_full_size(engine, frame):
-    """The fused schedule (split rows, costs computed in the first halves) at
-    full size, through the host-buffer and the device-buffer calls, against
-    the checker and against the other schedules' device maps."""
+    """The schedules that split the rows (FUSED: costs computed in the first
+    halves; SPLIT: first halves beside the vertical passes) at full size,
+    through the host-buffer and the device-buffer calls, against the checker."""
     import torch
     from conftest import reference_plain
     W, H, D, paths = frame
@@ -335,7 +339,7 @@ def test_fused_schedule_full_size(engine, frame):
     want = reference_plain(left, right, D, paths)
     engine.plan(W, H, D, paths)
     try:
-        for sched in (sgmgb.SCHED_FUSED, sgmgb.SCHED_THROUGHPUT):
+        for sched in (sgmgb.SCHED_FUSED, sgmgb.SCHED_SPLIT, sgmgb.SCHED_THROUGHPUT):
             engine.set_schedule(sched)
             got = engine.run_frame(left, right)
             assert np.array_equal(got, want), ("host", sched) + (_first_diff(got, want),)
