@@ -237,7 +237,6 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     const int hw = P.W >> 1;
 
     uint32_t dacc[2][KW];                             // FINAL3H: the chunk's disparities of rows A and B, byte k = step k
-    uint32_t tots[FIN ? K : 1][NR];                   // final modes: each step's totals, for the chunk's argmins
     // one step of both lines; `row`: this step's cost row in the chunk; kk: the step within the chunk
     auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&ps)[NR], const uint32_t (&sv)[NR], uint8_t *row,
                          int i, int kk, auto full_t) {
@@ -298,16 +297,8 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             }
             return;
         }
-        // final passes: the argmin waits for the chunk's end (below), so that
-        // its reductions stay off the recurrence's per-step dependency chain
-#pragma unroll
-        for (int j = 0; j < NR; j++) tots[FIN ? kk : 0][j] = tot[j];
-    };
-
-    // The argmins of a chunk's steps (FIN modes): d minimising the total over
-    // the lanes' disparities, the lowest d winning ties; every lane reaches the
-    // reductions, and all of them hold da and db.
-    auto argmin_of = [&](const uint32_t (&tot)[NR], uint32_t &da, uint32_t &db) {
+        // final passes: argmin over d, the lowest d winning ties; every lane reaches the reductions
+        uint32_t da, db;
         if (KEY16) {
             uint32_t k = kFull;
 #pragma unroll
@@ -324,6 +315,22 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             }
             da = __reduce_min_sync(kFull, ka) & 0xFFu;
             db = __reduce_min_sync(kFull, kb) & 0xFFu;
+        }
+        if (MODE == MODE_FINAL3H) {                   // every lane holds da and db: gather them per chunk
+            dacc[0][kk >> 2] |= da << (8 * (kk & 3));
+            dacc[1][kk >> 2] |= db << (8 * (kk & 3));
+            return;
+        }
+        if (lane == 0) {
+            if (MODE == MODE_FINAL && P.even_only) {  // multi-scale: the map at (2x, 2y) only
+                if (live_a && !((xa | ya) & 1)) P.disp[(long long)(ya >> 1) * hw + (xa >> 1)] = (uint8_t)da;
+                if (live_b && !((xb | yb) & 1)) P.disp[(long long)(yb >> 1) * hw + (xb >> 1)] = (uint8_t)db;
+            } else if (pair_store) {
+                if (live_a) *(uint16_t *)(P.disp + pa) = (uint16_t)(da | (db << 8));
+            } else {
+                if (live_a) P.disp[pa] = (uint8_t)da;
+                if (live_b) P.disp[pb] = (uint8_t)db;
+            }
         }
     };
 
@@ -360,46 +367,16 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             }
         }
         const long long pa0 = pa + step, pb0 = pb + step;   // the chunk's first pixel of each line
-        const int xa0 = xa + dx, ya0 = ya + dy, xb0 = xb + dx, yb0 = yb + dy;
+        if (MODE == MODE_FINAL3H) {
+#pragma unroll
+            for (int w = 0; w < KW; w++) dacc[0][w] = dacc[1][w] = 0u;
+        }
         if ((ch + 1) * K <= minlen) {
 #pragma unroll
             for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, k, std::true_type{});
         } else {
 #pragma unroll
             for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, k, std::false_type{});
-        }
-        if (FIN) {
-            if (MODE == MODE_FINAL3H) {
-#pragma unroll
-                for (int w = 0; w < KW; w++) dacc[0][w] = dacc[1][w] = 0u;
-            }
-            const int nlive = min(K, maxlen - ch * K);         // warp-uniform, >= 1
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                if (k >= nlive) break;
-                uint32_t da, db;
-                argmin_of(tots[FIN ? k : 0], da, db);
-                if (MODE == MODE_FINAL3H) {                    // gathered per row, stored once per chunk below
-                    dacc[0][k >> 2] |= da << (8 * (k & 3));
-                    dacc[1][k >> 2] |= db << (8 * (k & 3));
-                    continue;
-                }
-                if (lane == 0) {
-                    const int i = ch * K + k;
-                    const bool live_a = i < lena, live_b = i < lenb;
-                    const long long pak = pa0 + (long long)k * step, pbk = pb0 + (long long)k * step;
-                    if (MODE == MODE_FINAL && P.even_only) {   // multi-scale: the map at (2x, 2y) only
-                        const int xak = xa0 + k * dx, yak = ya0 + k * dy, xbk = xb0 + k * dx, ybk = yb0 + k * dy;
-                        if (live_a && !((xak | yak) & 1)) P.disp[(long long)(yak >> 1) * hw + (xak >> 1)] = (uint8_t)da;
-                        if (live_b && !((xbk | ybk) & 1)) P.disp[(long long)(ybk >> 1) * hw + (xbk >> 1)] = (uint8_t)db;
-                    } else if (pair_store) {
-                        if (live_a) *(uint16_t *)(P.disp + pak) = (uint16_t)(da | (db << 8));
-                    } else {
-                        if (live_a) P.disp[pak] = (uint8_t)da;
-                        if (live_b) P.disp[pbk] = (uint8_t)db;
-                    }
-                }
-            }
         }
         if (MODE == MODE_FINAL3H && lane == 0) {
             // row r's live steps of the chunk go to disp[p0 + dx*k]: one word store per 4 steps
