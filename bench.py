@@ -587,7 +587,7 @@ def run_gb300(args):
     e1s.record(s)
     torch.cuda.synchronize(dev)
     serial_ms_per_frame = e0s.elapsed_time(e1s) / n_serial
-    eng.set_schedule(sgmgb.SCHED_AUTO)   # frames in flight: the throughput schedule
+    eng.set_schedule(sgmgb.SCHED_AUTO)   # frames in flight: the fused schedule
     run_frames(args.warmup, NF)
     torch.cuda.synchronize(dev)
 
@@ -661,8 +661,8 @@ def run_gb300(args):
     pg_exact = bool(np.array_equal(plug.run(pl[0], pr[0])[1], maps0[0]))
 
     # per-kernel device time, each kernel alone, CUDA events on the engine's
-    # stream: the throughput schedule (`value`) and the latency one (`e2e`)
-    eng.set_schedule(sgmgb.SCHED_THROUGHPUT)
+    # stream: the fused schedule (`value`) and the latency one (`e2e`)
+    eng.set_schedule(sgmgb.SCHED_FUSED)
     kstats = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
     eng.set_schedule(sgmgb.SCHED_LATENCY)
     kstats_lat = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
@@ -684,7 +684,7 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u16", "data": "synthetic",
         "config": workload_config(ws),
-        "run": {"frames_in_flight": NF, "schedule": "throughput (frames in flight)",
+        "run": {"frames_in_flight": NF, "schedule": "fused (frames in flight)",
                 "inputs": "resident on the device; per-frame working set 570 MB > L2"},
         "frame_latency_ms": serial_ms_per_frame,
         "fps": ws * args.steps / (ms / 1e3),
@@ -708,7 +708,7 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": top[2],
                      "launch_ms": top[1],
-                     "note": "dominant kernel of the throughput-schedule frame (longest mean launch, timed alone "
+                     "note": "dominant kernel of the fused-schedule frame (longest mean launch, timed alone "
                              "with CUDA events); "
                              "achieved = its algorithmic bytes per launch / that time; peak = %s HBM copy "
                              "bandwidth; traffic = ncu dram bytes of one launch (profiles/)" % peak_kind},

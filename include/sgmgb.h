@@ -115,8 +115,9 @@ int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane
  *               directions: the shortest critical path of the four. Same
  *               frames as FUSED; other frames run THROUGHPUT;
  *   AUTO        LATENCY for sgmgb_run_frame and for a server frame with
- *               nothing else in flight, THROUGHPUT for sgmgb_run_frame_async
- *               and the other server frames (the default).
+ *               nothing else in flight, FUSED (THROUGHPUT where FUSED does not
+ *               apply) for sgmgb_run_frame_async and the other server frames
+ *               (the default).
  * Drops cached graphs. */
 #define SGMGB_SCHED_AUTO       0
 #define SGMGB_SCHED_LATENCY    1

@@ -182,3 +182,20 @@ def test_cli_plain_cost_gate(tmp_path):
     assert p.returncode == 3 and "ROOFLINE FAIL" in p.stderr
     p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-n", 3, "--board", "other", "--roofline-cal", cal)
     assert p.returncode == 0 and "NOT ARMED" in p.stderr              # no row for this board: says so
+
+
+@pytest.mark.gpu
+def test_cli_plain_default_calibration_arms_on_the_reference_scene(tmp_path):
+    """The gb300 calibration rows shipped beside the package (recorded with
+    --roofline-calibrate on the reference's calibration scene, gen_synthetic
+    1920x1080 seed 1, as its Makefile's roofline-cal target does) arm the gate
+    on that scene; the map is the committed golden (FNV 0bc0102058d1505f)."""
+    l, r, _ = oracle.gen_reference(1920, 1080, 64, 1)
+    write_pgm(str(tmp_path / "l.pgm"), l)
+    write_pgm(str(tmp_path / "r.pgm"), r)
+    p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-w", 2, "-n", 9, "--roofline-max", 2.0,
+            "-j", tmp_path / "res.jsonl")
+    assert p.returncode == 0, p.stdout + p.stderr
+    assert "NOT ARMED" not in p.stderr and "roofline:" in p.stdout
+    assert HARNESS_LINE.match(p.stdout.splitlines()[0]).group(15) == "0bc0102058d1505f"
+    assert json.loads(open(tmp_path / "res.jsonl").read())["roofline_ok"] == 1
