@@ -67,18 +67,23 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def committed_traffic(kernel):
-    """DRAM bytes (read + write) of one launch of `kernel` at configuration A,
-    from the committed ncu summary (lines "traffic <kernel> <bytes>"), or None."""
+def committed_profile(kind, kernel):
+    """DRAM bytes ("traffic": read + write) or warp-instructions
+    ("instructions") of one launch of `kernel` at configuration A, from the
+    committed ncu summary (lines "<kind> <kernel> <count>"), or None."""
     path = os.path.join(ROOT, "profiles", "configA_kernel_traffic.txt")
     try:
         for line in open(path):
             f = line.split()
-            if len(f) >= 3 and f[0] == "traffic" and f[1] == kernel:
+            if len(f) >= 3 and f[0] == kind and f[1] == kernel:
                 return int(f[2])
     except Exception:
         pass
     return None
+
+
+def committed_traffic(kernel):
+    return committed_profile("traffic", kernel)
 
 
 class ClockSampler:
@@ -678,6 +683,11 @@ def run_gb300(args):
     top = max(kstats, key=lambda k: k[1])
     achieved = top[2] / (top[1] / 1e3) / 1e9
     traffic = committed_traffic(top[0])
+    top_inst = committed_profile("instructions", top[0])
+    frame_inst = sum(committed_profile("instructions", k[0]) or 0 for k in kstats) or None
+    frame_traffic = sum(committed_traffic(k[0]) or 0 for k in kstats) or None
+    clk = clocks.summary(tw0, tw1)
+    issue_peak = 4 * torch.cuda.get_device_properties(dev).multi_processor_count * (clk["sm_mhz"] or 2070.0) * 1e6
     frame_ms_alone = sum(k[1] for k in kstats)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -714,12 +724,26 @@ def run_gb300(args):
                              "bandwidth; traffic = ncu dram bytes of one launch (profiles/)" % peak_kind},
         "frame_roofline": {"modelled_bytes": B_ALG, "achieved": B_ALG / (ms_per_step / 1e3) / 1e9,
                            "frac": B_ALG / (ms_per_step / 1e3) / 1e9 / peak, "unit": "GB/s",
-                           "note": "B_alg = 2*W*H*D + 3*W*H over the pipelined frame time (ms_per_step)"},
+                           "measured_bytes": frame_traffic,
+                           "measured_over_modelled": frame_traffic / B_ALG if frame_traffic else None,
+                           "measured_frac": (frame_traffic / (ms_per_step / 1e3) / 1e9 / peak) if frame_traffic
+                           else None,
+                           "note": "B_alg = 2*W*H*D + 3*W*H over the pipelined frame time (ms_per_step); "
+                                   "measured_bytes: ncu dram bytes of one frame's kernels (profiles/)"},
+        "issue_roofline": {"kernel": top[0], "warp_instructions": top_inst,
+                           "achieved": top_inst / (top[1] / 1e3) if top_inst else None,
+                           "peak": issue_peak, "unit": "warp-instructions/s",
+                           "frac": top_inst / (top[1] / 1e3) / issue_peak if top_inst else None,
+                           "frame_warp_instructions": frame_inst,
+                           "frame_frac": frame_inst / (ms_per_step / 1e3) / issue_peak if frame_inst else None,
+                           "note": "the recurrence is 8/16-bit integer work on the issue slots: peak = 4 schedulers "
+                                   "x SMs x the SM clock sampled in the timed region; instructions from ncu "
+                                   "(profiles/), time from the live CUDA-event timing"},
         "kernels": [{"name": k[0], "ms": round(k[1], 5), "algorithmic_bytes": k[2],
                      "gbs": round(k[2] / (k[1] / 1e3) / 1e9, 1)} for k in kstats],
         "frame_ms_kernels_alone": frame_ms_alone,
         "cpu_baseline": None,
-        "clocks": clocks.summary(tw0, tw1),
+        "clocks": clk,
         "gpu_launches": args.steps * KERNELS_PER_FRAME,
     }
     for e in engines:
