@@ -204,6 +204,9 @@ def batched_section(eng_cls, sgmgb, torch, np):
     maps = [o.cpu().numpy() for o in out]
     same = all(np.array_equal(m, rf) for m, rf in zip(maps, ref))
     shapes = sorted(set(b.tile_shape(i) for i in range(len(specs))))
+    busy = b.busy()
+    busy_ms = {k: busy[k] for k in sgmgb.Batch.BUSY_KINDS}
+    blocks = busy["blocks"]
     for e in engs.values():
         e.close()
     b.close()
@@ -223,6 +226,13 @@ def batched_section(eng_cls, sgmgb, torch, np):
             "sequential_dropin_ms": seq_ms, "sequential_dropin_fps": 96e3 / seq_ms,
             "speedup_vs_sequential_dropin": seq_ms / batch_ms, "identical_to_dropin": bool(same),
             "frames_equal_to_their_checked_class_frame": covered,
+            "block_time_ms": {k: round(v, 3) for k, v in busy_ms.items()},
+            "block_time_share": {k: round(v / max(1e-9, sum(busy_ms.values())), 4) for k, v in busy_ms.items()},
+            "blocks": blocks,
+            "busy_per_block_over_run": sum(busy_ms.values()) / blocks / batch_ms,
+            "block_time_note": "time the persistent kernel's blocks spent per work-item kind in the last run "
+                               "(clock64 stamps, summed over blocks, at the maximum SM clock); 'wait' is time "
+                               "spent waiting for an item's inputs or on an empty queue",
             "launches_per_batch": 1, "tile_shapes_warps_dpl": shapes,
             "note": "one persistent launch per batch (CUDA graph); batch inputs resident on the device; "
                     "drop-in calls copy host buffers in and out"}, checks

@@ -197,8 +197,10 @@ int sgmgb_run_frame_noalloc(const uint8_t *d_left, const uint8_t *d_right, uint8
  * row bands, cost row bands, groups of lines of one direction) from a device
  * queue in phase order and wait, with a bounded spin, on per-frame phase
  * counters. The launch and its counter resets are captured in a CUDA graph on
- * the first run and replayed afterwards. Outputs are bit-identical to
- * sgmgb_run_frame on each frame. */
+ * the first run and replayed afterwards. Frames with 4 paths in the
+ * two-lines-per-warp layout (D = 32, 64, 128) run the fused schedule's items
+ * (SGMGB_SCHED_FUSED), the others the throughput schedule's. Outputs are
+ * bit-identical to sgmgb_run_frame on each frame. */
 typedef struct sgmgb_batch sgmgb_batch;
 /* Plans n frames: one workspace arena, the work-item queue and its phase
  * counters. tune_cache (may be NULL) is an autotuner cache file (see below):
@@ -223,6 +225,15 @@ int  sgmgb_batch_wait(sgmgb_batch *b);
 int  sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left,
                           const uint8_t *const *d_right, uint8_t *const *d_disp,
                           const char *tune_cache);
+/* Where the last run's time went (no reference symbol): ms[k] is the time
+ * the persistent kernel's blocks spent on work items of kind k, summed over
+ * blocks, in milliseconds at the SM's maximum clock: k = 0 census, 1 cost,
+ * 2 passes that park a direction's L, 3 final passes (planes added, argmin),
+ * 4 first halves of split rows with their costs, 5 waiting for an item's
+ * inputs (or for the queue to end). n <= 6 entries are filled (more are set
+ * to 0); *blocks (may be NULL) receives the launch's block count, so that
+ * sum(ms) / blocks is about the run's time. Waits for the last run. */
+int  sgmgb_batch_busy(sgmgb_batch *b, double *ms, int n, int *blocks);
 /* Path-kernel shape used for frame i: warps per block and disparities per lane. */
 int  sgmgb_batch_tile_shape(const sgmgb_batch *b, int i, int *warps_per_block,
                             int *disp_per_lane);

@@ -2,7 +2,14 @@
 //
 // Work decomposition (plain variant, common/sgm_ref.c semantics per frame):
 //   phase 0  census   one item per band of BAND (8) rows (both images)
-//   phase 1  cost     one item per band: C[p][d] from the band's census rows
+//   4 paths, two lines per warp (D = 32, 64, 128), the fused schedule:
+//            phase 1  the first halves of L->R and R->L with their costs
+//                     computed from the census (sgmgb_fused.cuh): the cost
+//                     volume, one plane of L and each row's line state
+//            phase 2  T->B and B->T into two u8 planes
+//            phase 3  the second halves of L->R and R->L add the three planes
+//                     to their L and take the argmin
+//   otherwise phase 1  cost: one item per band, C[p][d] from its census rows
 //   4 paths: phase 2  R->L, B->T, L->R into three u8 planes (all three passes)
 //            phase 3  T->B adds the planes to its L and takes the argmin
 //   8 paths: phase 2  R->L, L->R, B->T and the four diagonals into seven planes
@@ -14,11 +21,19 @@
 // that no running block holds.
 //
 // Cross-block data (census, cost, planes, sums) is read through L2 only
-// (cp.async.cg, ld.global.cg): a block never reads such data through its L1.
+// (cp.async.cg, ld.global.cg), with one exception: the first-half items copy
+// the census descriptors with 8-byte cp.async.ca, through L1. That is safe
+// because L1 holds no line from before the launch, and no block reads a
+// frame's descriptors before every census item of that frame has finished
+// (the item's acquire and block barrier) -- after which they do not change.
+//
+// Every item's busy time and its wait for its inputs are accumulated per item
+// kind from clock64 stamps into the control block (sgmgb_batch_busy).
 #include "sgmgb_internal.h"
 #include "sgmgb_path.cuh"
 #include "sgmgb_tiles.cuh"
 #include "sgmgb_pair.cuh"
+#include "sgmgb_fused.cuh"
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -32,7 +47,11 @@ namespace {
 constexpr int BAND = tiles::CEN_ROWS;   // rows per census / cost item
 constexpr int MAXPH = 4;         // phases per frame: census, cost, scratch passes, final pass
 
-enum ItemKind : int { IT_CENSUS = 0, IT_COST = 1, IT_PATH = 2 };
+enum ItemKind : int { IT_CENSUS = 0, IT_COST = 1, IT_PATH = 2, IT_HCOST = 3 };
+// busy-time kinds (BCtl::busy): census, cost, passes that park L, final
+// passes, first halves with costs, and the waits for inputs
+enum BusyKind : int { BK_CENSUS = 0, BK_COST = 1, BK_SCRATCH = 2, BK_FINAL = 3, BK_HCOST = 4, BK_WAIT = 5,
+                      BK_N = 6 };
 
 struct BFrame {                  // per frame; the user pointers are refreshed per run
     const uint8_t *left, *right;
@@ -62,6 +81,7 @@ struct BCtl {                    // device control block, reset before every run
     unsigned abort;              // set on a wait timeout: every block stops taking items
     int err_item;                // item whose wait ran out (-1: none)
     unsigned pad;
+    unsigned long long busy[BK_N];   // SM-clock cycles summed over items, per BusyKind
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
@@ -131,6 +151,9 @@ __device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int wa
         case 4 * 8 + MODE_STORE:   path_pair<4, MODE_STORE, 0, false>(P, warp, ring); break;
         case 4 * 8 + MODE_ACCUM:   path_pair<4, MODE_ACCUM, 0, false>(P, warp, ring); break;
         case 4 * 8 + MODE_FINAL:   path_pair<4, MODE_FINAL, 0, false>(P, warp, ring); break;
+        case 1 * 8 + MODE_FINAL3H: path_pair<1, MODE_FINAL3H, 0, true>(P, warp, ring); break;
+        case 2 * 8 + MODE_FINAL3H: path_pair<2, MODE_FINAL3H, 0, true>(P, warp, ring); break;
+        case 4 * 8 + MODE_FINAL3H: path_pair<4, MODE_FINAL3H, 0, false>(P, warp, ring); break;
         default:                   path_pair<4, MODE_FINAL3, 0, false>(P, warp, ring); break;
         }
         return;
@@ -164,19 +187,35 @@ __device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int wa
     }
 }
 
+// One warp's share of a first-half item: row pair `pair` of pass `bp` (its
+// P.dx gives the direction).
+__device__ __forceinline__ void item_hcost(const BPass &bp, int pair, uint8_t *ring) {
+    uint64_t *ws = (uint64_t *)ring;
+    const bool lr = bp.P.dx > 0;
+    switch (bp.P.D) {
+    case 32:  if (lr) path_hcost<1, 1>(bp.P, pair, ws); else path_hcost<1, -1>(bp.P, pair, ws); break;
+    case 64:  if (lr) path_hcost<2, 1>(bp.P, pair, ws); else path_hcost<2, -1>(bp.P, pair, ws); break;
+    default:  if (lr) path_hcost<4, 1>(bp.P, pair, ws); else path_hcost<4, -1>(bp.P, pair, ws); break;
+    }
+}
+
 // The persistent batch kernel: every block loops taking the next queued item
 // until the queue is empty or the run is aborted. `ring_bytes`: one warp's
 // path ring; the census and cost items use the start of the block's memory.
-__global__ void __launch_bounds__(256)
+// At most 128 registers, so that two 256-thread (four 128-thread) blocks fit
+// an SM whatever item kinds are inlined.
+__global__ void __launch_bounds__(256, 2)
 k_batch(const BItem *__restrict__ items, int n_items, const BFrame *__restrict__ frames,
         const BPass *__restrict__ passes, unsigned *done, const unsigned *__restrict__ need,
         BCtl *ctl, int ring_bytes, long long limit_cycles) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ int s_item;
     const int wib = threadIdx.x >> 5;
+    long long t_ready = 0;                       // thread 0: when the item's inputs were there
     for (;;) {
         if (threadIdx.x == 0) {
             int it = ld_acquire(&ctl->abort) ? n_items : (int)atomicAdd(&ctl->next, 1u);
+            const long long t_take = clock64();
             if (it < n_items) {
                 const BItem I = items[it];
                 if (I.phase > 0) {
@@ -184,6 +223,8 @@ k_batch(const BItem *__restrict__ items, int n_items, const BFrame *__restrict__
                     if (!wait_count(&done[c], need[c], ctl, it, limit_cycles)) it = n_items;
                 }
             }
+            t_ready = clock64();
+            atomicAdd(&ctl->busy[BK_WAIT], (unsigned long long)(t_ready - t_take));
             s_item = it;
         }
         __syncthreads();
@@ -193,12 +234,17 @@ k_batch(const BItem *__restrict__ items, int n_items, const BFrame *__restrict__
         switch (I.kind) {
         case IT_CENSUS: item_census(frames[I.frame], I.arg, smem); break;
         case IT_COST:   item_cost(frames[I.frame], I.arg, smem); break;
+        case IT_HCOST:  item_hcost(passes[I.arg], I.sub + wib, smem + wib * ring_bytes); break;
         default:        item_path(passes[I.arg], frames[I.frame].disp, I.sub + wib, smem + wib * ring_bytes); break;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
             atomicAdd(&done[I.frame * MAXPH + I.phase], 1u);
+            const int m = I.kind == IT_PATH ? passes[I.arg].mode : -1;
+            const int kind = I.kind == IT_CENSUS ? BK_CENSUS : I.kind == IT_COST ? BK_COST
+                           : I.kind == IT_HCOST ? BK_HCOST : m == MODE_SCRATCH ? BK_SCRATCH : BK_FINAL;
+            atomicAdd(&ctl->busy[kind], (unsigned long long)(clock64() - t_ready));
         }
     }
 }
@@ -312,12 +358,58 @@ int build_plan(sgmgb_batch *b) {
         const sgmgb_frame_desc &fd = b->fds[f];
         const FrameSlot &s = b->slots[f];
         const int nb = (fd.H + BAND - 1) / BAND;
+        // 4 paths in the pair layout: the fused schedule (no cost items)
+        const bool fused = fd.paths == 4 && b->dpl[f] == 0 && pair_ok(fd.D);
         for (int k = 0; k < nb; k++) {
             by_phase[0].push_back({IT_CENSUS, f, 0, k, 0});
-            by_phase[1].push_back({IT_COST, f, 1, k, 0});
+            if (!fused) by_phase[1].push_back({IT_COST, f, 1, k, 0});
         }
         b->need[(size_t)f * MAXPH + 0] = nb;
-        b->need[(size_t)f * MAXPH + 1] = nb;
+        b->need[(size_t)f * MAXPH + 1] = fused ? 0 : nb;
+        if (fused) {
+            const size_t plane = (size_t)fd.W * fd.H * fd.D;
+            uint8_t *ph = s.sc, *ptb = (uint8_t *)s.S, *pbt = (uint8_t *)s.S + plane;
+            LineParams q{};
+            q.C = s.C; q.W = fd.W; q.H = fd.H; q.D = fd.D; q.p1 = 20; q.p2 = 192; q.dpl = 0; q.key16 = fd.D <= 64;
+            const int npairs = (fd.H + 1) / 2;
+            // phase 1: the first halves of L->R and R->L with their costs
+            for (int dx : {1, -1}) {
+                BPass bp{};
+                bp.P = q;
+                bp.P.dx = dx; bp.P.dy = 0; bp.P.hseg = 1; bp.P.cl = s.cl; bp.P.cr = s.cr; bp.P.sc = ph;
+                bp.P.state = s.state; bp.P.nlines = fd.H;
+                bp.frame = f; bp.mode = MODE_SCRATCH; bp.dpl = 0;
+                const int pi = (int)passes.size();
+                passes.push_back(bp);
+                const int nit = (npairs + b->wpb - 1) / b->wpb;
+                for (int j = 0; j < nit; j++) by_phase[1].push_back({IT_HCOST, f, 1, pi, j * b->wpb});
+                b->need[(size_t)f * MAXPH + 1] += nit;
+            }
+            ring = std::max(ring, fd.D == 32 ? HCost<1>::BYTES : fd.D == 64 ? HCost<2>::BYTES : HCost<4>::BYTES);
+            // phase 2: T->B and B->T into two planes; phase 3: the second halves
+            struct FSpec { int dx, dy, mode, phase, hseg; uint8_t *sc; const uint8_t *sc2, *sc3; };
+            const FSpec fs[4] = {{0, 1, MODE_SCRATCH, 2, 0, ptb, nullptr, nullptr},
+                                 {0, -1, MODE_SCRATCH, 2, 0, pbt, nullptr, nullptr},
+                                 {1, 0, MODE_FINAL3H, 3, 2, ph, ptb, pbt},
+                                 {-1, 0, MODE_FINAL3H, 3, 2, ph, ptb, pbt}};
+            for (const FSpec &sp : fs) {
+                BPass bp{};
+                bp.P = q;
+                bp.P.dx = sp.dx; bp.P.dy = sp.dy; bp.P.hseg = sp.hseg;
+                bp.P.sc = sp.sc; bp.P.sc2 = sp.sc2; bp.P.sc3 = sp.sc3;
+                bp.P.state = sp.hseg ? s.state : nullptr;
+                bp.P.nlines = lines_for(fd.W, fd.H, sp.dx, sp.dy);
+                bp.frame = f; bp.mode = sp.mode; bp.dpl = 0;
+                const int pi = (int)passes.size();
+                passes.push_back(bp);
+                ring = std::max(ring, pair_ring_bytes(fd.D, sp.mode));
+                const int warps = (bp.P.nlines + 1) / 2;
+                const int nit = (warps + b->wpb - 1) / b->wpb;
+                for (int j = 0; j < nit; j++) by_phase[sp.phase].push_back({IT_PATH, f, sp.phase, pi, j * b->wpb});
+                b->need[(size_t)f * MAXPH + sp.phase] += nit;
+            }
+            continue;
+        }
         LineParams base{};
         base.C = s.C; base.sc = s.sc; base.S = s.S; base.disp = nullptr;
         base.W = fd.W; base.H = fd.H; base.D = fd.D; base.p1 = 20; base.p2 = 192;
@@ -581,6 +673,24 @@ done:
                 return berr(b, SGMGB_ERR_STATE, std::string("cannot append to tune cache ") + tune_cache);
         }
     }
+    return SGMGB_OK;
+}
+
+int sgmgb_batch_busy(sgmgb_batch *b, double *ms, int n, int *blocks) {
+    if (!b || !ms || n < 1) return SGMGB_ERR_ARG;
+    if (!b->ran) return berr(b, SGMGB_ERR_STATE, "the batch has not run");
+    cudaSetDevice(b->ctx->device);
+    if (cudaEventSynchronize(b->done_ev) != cudaSuccess) {
+        cudaGetLastError();
+        return berr(b, SGMGB_ERR_CUDA, "batch run");
+    }
+    int khz = 0;
+    if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, b->ctx->device) != cudaSuccess || khz <= 0) {
+        cudaGetLastError();
+        return berr(b, SGMGB_ERR_CUDA, "SM clock rate");
+    }
+    for (int k = 0; k < n; k++) ms[k] = k < BK_N ? (double)b->h_ctl[1].busy[k] / khz : 0.0;
+    if (blocks) *blocks = b->grid;
     return SGMGB_OK;
 }
 

@@ -34,7 +34,7 @@ EXPORTS = [
     "sgmgb_batch_destroy", "sgmgb_tune_lookup", "sgmgb_tune_record",
     "sgmgb_server_create", "sgmgb_server_add_camera", "sgmgb_server_submit", "sgmgb_server_poll",
     "sgmgb_server_wait", "sgmgb_server_stats_get", "sgmgb_server_destroy", "sgmgb_synth_pair",
-    "sgmgb_server_prepare",
+    "sgmgb_server_prepare", "sgmgb_batch_busy",
     "sgmgb_run_frame_noalloc",
 ]
 
@@ -103,6 +103,7 @@ def _load():
         "sgmgb_batch_autotune": (i, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
                                      ctypes.c_char_p]),
         "sgmgb_batch_tile_shape": (i, [vp, i, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "sgmgb_batch_busy": (i, [vp, ctypes.POINTER(ctypes.c_double), i, ctypes.POINTER(i)]),
         "sgmgb_batch_set_fault": (i, [vp, i, i]),
         "sgmgb_batch_destroy": (None, [vp]),
         "sgmgb_tune_lookup": (i, [ctypes.c_char_p, fdp, ctypes.POINTER(i), ctypes.POINTER(i)]),
@@ -314,6 +315,18 @@ class Batch:
     def autotune(self, d_lefts, d_rights, d_disps, tune_cache=None):
         self.engine._check(lib.sgmgb_batch_autotune(self.h, *self._arrays(d_lefts, d_rights, d_disps),
                                                     _cstr(tune_cache)))
+
+    BUSY_KINDS = ("census", "cost", "scratch", "final", "first_half_cost", "wait")
+
+    def busy(self):
+        """Milliseconds the last run's blocks spent per work-item kind (summed
+        over blocks), and the block count under "blocks"."""
+        out = (ctypes.c_double * 6)()
+        nb = ctypes.c_int()
+        self.engine._check(lib.sgmgb_batch_busy(self.h, out, 6, ctypes.byref(nb)))
+        d = {k: out[i] for i, k in enumerate(self.BUSY_KINDS)}
+        d["blocks"] = nb.value
+        return d
 
     def tile_shape(self, i):
         """(warps per block, disparities per lane) used for frame i."""

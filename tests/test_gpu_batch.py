@@ -159,3 +159,31 @@ def test_batch_baseline_sizes(engine, baseline_frames):
                                 % (run, k, int((got != want).sum()), x, y, got[y, x], want[y, x]))
     finally:
         b.close()
+
+
+def test_batch_busy_accounts_for_the_run(engine):
+    """sgmgb_batch_busy: the blocks' time by item kind. A batch with a fused
+    frame (4 paths, D = 64) and an 8-path frame has census, first-half, cost,
+    scratch and final work; the kinds' sum per block cannot exceed the run's
+    time on the device (blocks that find the queue empty leave at once)."""
+    import torch
+    specs = [(320, 240, 64, 4), (200, 120, 64, 8)]
+    descs, host, dev, outs = _frames(specs, seed0=50)
+    b = sgmgb.Batch(engine, descs)
+    L, R = [d[0] for d in dev], [d[1] for d in dev]
+    b.run(L, R, outs)
+    b.wait()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.run(L, R, outs)
+    e1.record()
+    b.wait()
+    torch.cuda.synchronize()
+    _check(host, outs, descs)
+    busy = b.busy()
+    for k in ("census", "cost", "scratch", "final", "first_half_cost"):
+        assert busy[k] > 0, (k, busy)
+    assert busy["wait"] >= 0 and busy["blocks"] > 0
+    per_block = sum(busy[k] for k in sgmgb.Batch.BUSY_KINDS) / busy["blocks"]
+    assert 0 < per_block < 1.5 * e0.elapsed_time(e1), (per_block, e0.elapsed_time(e1))
+    b.close()
