@@ -231,7 +231,7 @@ def batched_section(eng_cls, sgmgb, torch, np):
             "blocks": blocks,
             "busy_per_block_over_run": sum(busy_ms.values()) / blocks / batch_ms,
             "block_time_note": "time the persistent kernel's blocks spent per work-item kind in the last run "
-                               "(clock64 stamps, summed over blocks, at the maximum SM clock); 'wait' is time "
+                               "(global-timer stamps, summed over blocks); 'wait' is time "
                                "spent waiting for an item's inputs or on an empty queue",
             "launches_per_batch": 1, "tile_shapes_warps_dpl": shapes,
             "note": "one persistent launch per batch (CUDA graph); batch inputs resident on the device; "

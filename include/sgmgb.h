@@ -227,7 +227,7 @@ int  sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left,
                           const char *tune_cache);
 /* Where the last run's time went (no reference symbol): ms[k] is the time
  * the persistent kernel's blocks spent on work items of kind k, summed over
- * blocks, in milliseconds at the SM's maximum clock: k = 0 census, 1 cost,
+ * blocks, in milliseconds of the GPU's global timer: k = 0 census, 1 cost,
  * 2 passes that park a direction's L, 3 final passes (planes added, argmin),
  * 4 first halves of split rows with their costs, 5 waiting for an item's
  * inputs (or for the queue to end). n <= 6 entries are filled (more are set

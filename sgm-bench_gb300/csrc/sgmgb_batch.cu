@@ -28,7 +28,7 @@
 // (the item's acquire and block barrier) -- after which they do not change.
 //
 // Every item's busy time and its wait for its inputs are accumulated per item
-// kind from clock64 stamps into the control block (sgmgb_batch_busy).
+// kind from global-timer stamps into the control block (sgmgb_batch_busy).
 #include "sgmgb_internal.h"
 #include "sgmgb_path.cuh"
 #include "sgmgb_tiles.cuh"
@@ -81,8 +81,15 @@ struct BCtl {                    // device control block, reset before every run
     unsigned abort;              // set on a wait timeout: every block stops taking items
     int err_item;                // item whose wait ran out (-1: none)
     unsigned pad;
-    unsigned long long busy[BK_N];   // SM-clock cycles summed over items, per BusyKind
+    unsigned long long busy[BK_N];   // nanoseconds summed over items, per BusyKind
 };
+
+// Nanoseconds of the GPU's global timer (busy-time stamps).
+__device__ __forceinline__ unsigned long long gtime_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     unsigned v;
@@ -94,13 +101,13 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 // passes (then records the item and aborts the run). Returns false if the
 // item must not run.
 __device__ bool wait_count(const unsigned *cnt, unsigned need, BCtl *ctl, int item,
-                           long long limit_cycles) {
+                           long long limit_ns) {
     if (ld_acquire(cnt) >= need) return true;
-    const long long t0 = clock64();
+    const unsigned long long t0 = gtime_ns();
     for (unsigned it = 0;; it++) {
         if (ld_acquire(&ctl->abort)) return false;
         if (ld_acquire(cnt) >= need) return true;
-        if (clock64() - t0 > limit_cycles || it > (1u << 26)) {
+        if ((long long)(gtime_ns() - t0) > limit_ns || it > (1u << 26)) {
             atomicCAS(&ctl->err_item, -1, item);
             atomicExch(&ctl->abort, 1u);
             return false;
@@ -207,24 +214,24 @@ __device__ __forceinline__ void item_hcost(const BPass &bp, int pair, uint8_t *r
 __global__ void __launch_bounds__(256, 2)
 k_batch(const BItem *__restrict__ items, int n_items, const BFrame *__restrict__ frames,
         const BPass *__restrict__ passes, unsigned *done, const unsigned *__restrict__ need,
-        BCtl *ctl, int ring_bytes, long long limit_cycles) {
+        BCtl *ctl, int ring_bytes, long long limit_ns) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ int s_item;
     const int wib = threadIdx.x >> 5;
-    long long t_ready = 0;                       // thread 0: when the item's inputs were there
+    unsigned long long t_ready = 0;              // thread 0: when the item's inputs were there
     for (;;) {
         if (threadIdx.x == 0) {
             int it = ld_acquire(&ctl->abort) ? n_items : (int)atomicAdd(&ctl->next, 1u);
-            const long long t_take = clock64();
+            const unsigned long long t_take = gtime_ns();
             if (it < n_items) {
                 const BItem I = items[it];
                 if (I.phase > 0) {
                     const int c = I.frame * MAXPH + I.phase - 1;
-                    if (!wait_count(&done[c], need[c], ctl, it, limit_cycles)) it = n_items;
+                    if (!wait_count(&done[c], need[c], ctl, it, limit_ns)) it = n_items;
                 }
             }
-            t_ready = clock64();
-            atomicAdd(&ctl->busy[BK_WAIT], (unsigned long long)(t_ready - t_take));
+            t_ready = gtime_ns();
+            atomicAdd(&ctl->busy[BK_WAIT], t_ready - t_take);
             s_item = it;
         }
         __syncthreads();
@@ -244,7 +251,7 @@ k_batch(const BItem *__restrict__ items, int n_items, const BFrame *__restrict__
             const int m = I.kind == IT_PATH ? passes[I.arg].mode : -1;
             const int kind = I.kind == IT_CENSUS ? BK_CENSUS : I.kind == IT_COST ? BK_COST
                            : I.kind == IT_HCOST ? BK_HCOST : m == MODE_SCRATCH ? BK_SCRATCH : BK_FINAL;
-            atomicAdd(&ctl->busy[kind], (unsigned long long)(clock64() - t_ready));
+            atomicAdd(&ctl->busy[kind], gtime_ns() - t_ready);
         }
     }
 }
@@ -502,10 +509,7 @@ void fill_frames(sgmgb_batch *b, const uint8_t *const *l, const uint8_t *const *
 int capture_graph(sgmgb_batch *b) {
     cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) { cudaGetLastError(); return berr(b, SGMGB_ERR_CUDA, "batch capture"); }
-    int clock_khz = 0;
-    cudaDeviceGetAttribute(&clock_khz, cudaDevAttrClockRate, b->ctx->device);
-    if (clock_khz <= 0) clock_khz = 2000000;
-    const long long limit = (long long)b->wait_limit_ms * clock_khz;
+    const long long limit = (long long)b->wait_limit_ms * 1000000LL;   // ns of the global timer
     cudaMemcpyAsync(b->d_frames, b->h_frames, sizeof(BFrame) * b->n, cudaMemcpyHostToDevice, b->cap);
     cudaMemsetAsync(b->d_done, 0, sizeof(unsigned) * b->need.size(), b->cap);
     cudaMemcpyAsync(b->d_ctl, &b->h_ctl[0], sizeof(BCtl), cudaMemcpyHostToDevice, b->cap);
@@ -684,12 +688,7 @@ int sgmgb_batch_busy(sgmgb_batch *b, double *ms, int n, int *blocks) {
         cudaGetLastError();
         return berr(b, SGMGB_ERR_CUDA, "batch run");
     }
-    int khz = 0;
-    if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, b->ctx->device) != cudaSuccess || khz <= 0) {
-        cudaGetLastError();
-        return berr(b, SGMGB_ERR_CUDA, "SM clock rate");
-    }
-    for (int k = 0; k < n; k++) ms[k] = k < BK_N ? (double)b->h_ctl[1].busy[k] / khz : 0.0;
+    for (int k = 0; k < n; k++) ms[k] = k < BK_N ? (double)b->h_ctl[1].busy[k] * 1e-6 : 0.0;
     if (blocks) *blocks = b->grid;
     return SGMGB_OK;
 }
