@@ -188,10 +188,11 @@ def batched_section(eng_cls, sgmgb, torch, np):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     reps = 5
-    e0.record()
+    s = torch.cuda.current_stream()
+    e0.record(s)
     for _ in range(reps):
-        b.run(dl, dr, out)
-    e1.record()
+        b.run(dl, dr, out, stream=s)           # on the stream the events are recorded on
+    e1.record(s)
     b.wait()
     torch.cuda.synchronize()
     batch_ms = e0.elapsed_time(e1) / reps

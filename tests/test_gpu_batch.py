@@ -174,9 +174,10 @@ def test_batch_busy_accounts_for_the_run(engine):
     b.run(L, R, outs)
     b.wait()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    b.run(L, R, outs)
-    e1.record()
+    s = torch.cuda.current_stream()
+    e0.record(s)
+    b.run(L, R, outs, stream=s)                    # on the stream the events are recorded on
+    e1.record(s)
     b.wait()
     torch.cuda.synchronize()
     _check(host, outs, descs)
