@@ -141,6 +141,26 @@ int sgmgb_run_frame_async(sgmgb_ctx *ctx, const uint8_t *d_left, const uint8_t *
 /* Waits for everything the context enqueued on `stream` (NULL = own stream). */
 int sgmgb_sync(sgmgb_ctx *ctx, void *stream);
 
+/* ---- optional post-steps (no reference counterpart) ---- */
+/* The reference has no post-steps (common/sgm_params.h:58). These are this
+ * engine's, on the plain variant's summed volume S (the frame runs the
+ * latency schedule; a second map and S cost an extra 2*W*H*D + 4*W*H bytes of
+ * device memory, made on the first call):
+ *   SGMGB_POST_LR        left-right consistency check: d_R(x) = argmin_d
+ *                        S(x + d, d); a pixel whose d satisfies x - d < 0 or
+ *                        |d - d_R(x - d)| > 1 becomes SGMGB_DISP_INVALID (D <= 240);
+ *   SGMGB_POST_MEDIAN    3x3 median of the (checked) map, edges replicated;
+ *   SGMGB_POST_SUBPIXEL  disp16 (W*H uint16) receives 16*d plus a parabola
+ *                        offset (16*(S(d-1) - S(d+1))) / (2*(S(d-1) + S(d+1) -
+ *                        2*S(d))) in integer arithmetic; 0xFFFF where checked out.
+ * Host buffers, synchronous. flags = 0 gives the plain map. */
+#define SGMGB_POST_LR        1
+#define SGMGB_POST_MEDIAN    2
+#define SGMGB_POST_SUBPIXEL  4
+#define SGMGB_DISP_INVALID   255
+int sgmgb_run_frame_post(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right, uint8_t *disp,
+                         uint16_t *disp16, int flags);
+
 /* ---- measurement (no reference symbol) ---- */
 typedef struct {
     char   name[24];   /* "census", "cost", "path_rl", ..., "sum_argmin" */

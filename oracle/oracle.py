@@ -59,6 +59,7 @@ def lib():
         L.sgmo_sobelx.argtypes = [vp, vp, i, i]
         L.sgmo_half.argtypes = [vp, vp, i, i]
         L.sgmo_gen_reference.argtypes = [i, i, i, ctypes.c_uint32, vp, vp, vp]
+        L.sgmo_post.argtypes = [vp, vp, i, i, i, i, i, vp, vp]
         L.sgmo_fnv1a64.argtypes = [vp, ctypes.c_size_t]
         L.sgmo_fnv1a64.restype = ctypes.c_uint64
         _lib = L
@@ -98,6 +99,23 @@ def multiscale(left, right):
     if rc:
         raise ValueError("oracle rejected multi-scale W=%d H=%d" % (W, H))
     return disp
+
+
+POST_LR, POST_MEDIAN, POST_SUBPIXEL = 1, 2, 4
+
+
+def post(left, right, D=64, paths=4, flags=0):
+    """The optional post-steps (no reference counterpart; defined in
+    sgm_oracle.c): (map, 16x subpixel map or None)."""
+    left = np.ascontiguousarray(left, np.uint8)
+    right = np.ascontiguousarray(right, np.uint8)
+    H, W = left.shape
+    disp = np.empty((H, W), np.uint8)
+    d16 = np.empty((H, W), np.uint16) if flags & POST_SUBPIXEL else None
+    rc = lib().sgmo_post(_p(left), _p(right), W, H, D, paths, flags, _p(disp), _p(d16) if d16 is not None else None)
+    if rc:
+        raise ValueError("oracle rejected post W=%d H=%d D=%d paths=%d flags=%d" % (W, H, D, paths, flags))
+    return disp, d16
 
 
 def gen_reference(W, H, D, seed):

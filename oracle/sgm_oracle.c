@@ -353,6 +353,81 @@ out:
     return rc;
 }
 
+/* Optional post-steps on the plain summed volume. The reference has none
+ * (common/sgm_params.h:58: "No LR check, no subpixel, no median"); these are
+ * this oracle's definitions, which the engine's post mode matches bit for bit:
+ *   d_L(p)   = argmin_d S(p, d), lowest d on ties (the plain map);
+ *   disp16   = 16*d_L + (16*(c0 - c2)) / (2*(c0 + c2 - 2*c1)) with c0, c1, c2 =
+ *              S(d_L - 1), S(d_L), S(d_L + 1), C integer division (toward zero),
+ *              when 0 < d_L < D-1 and the denominator is > 0; else 16*d_L;
+ *   LR:      d_R(x, y) = argmin over d with x + d < W of S((x + d, y), d),
+ *              lowest d on ties; p = (x, y) is invalid (255; disp16 0xFFFF)
+ *              when x - d_L < 0 or |d_L - d_R(x - d_L, y)| > 1;
+ *   median:  the 3x3 median of the (checked) map, edge-replicated. */
+static uint8_t median9(uint8_t *v)
+{
+    for (int i = 1; i < 9; i++)
+        for (int j = i; j > 0 && v[j - 1] > v[j]; j--) { uint8_t t = v[j]; v[j] = v[j - 1]; v[j - 1] = t; }
+    return v[4];
+}
+
+int sgmo_post(const uint8_t *left, const uint8_t *right, int W, int H, int D, int paths, int flags,
+              uint8_t *disp, uint16_t *disp16)
+{
+    if (!left || !right || !disp || W < 1 || H < 1 || (flags & ~7)) return -1;
+    if ((flags & SGMO_POST_LR) && D > 240) return -1;
+    if ((flags & SGMO_POST_SUBPIXEL) && !disp16) return -1;
+    const size_t N = (size_t)W * H;
+    uint16_t *S = malloc(N * (size_t)D * 2);
+    uint8_t *dL = malloc(N), *dR = malloc(N);
+    int rc = -1;
+    if (!S || !dL || !dR) goto out;
+    if (sgmo_plain(left, right, W, H, D, paths, dL, S)) goto out;
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            int best = 0, bv = 1 << 30;
+            for (int d = 0; d < D && x + d < W; d++) {
+                const int v = S[((size_t)y * W + x + d) * D + d];
+                if (v < bv) { bv = v; best = d; }
+            }
+            dR[(size_t)y * W + x] = (uint8_t)best;
+        }
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            const size_t i = (size_t)y * W + x;
+            const int d = dL[i];
+            const uint16_t *s = S + i * D;
+            int v16 = 16 * d;
+            if (d > 0 && d < D - 1) {
+                const int c0 = s[d - 1], c1 = s[d], c2 = s[d + 1], den = c0 + c2 - 2 * c1;
+                if (den > 0) v16 += (16 * (c0 - c2)) / (2 * den);
+            }
+            int out = d;
+            if (flags & SGMO_POST_LR) {
+                const int xr = x - d;
+                if (xr < 0 || abs(d - (int)dR[(size_t)y * W + xr]) > 1) { out = 255; v16 = 0xFFFF; }
+            }
+            disp[i] = (uint8_t)out;
+            if (flags & SGMO_POST_SUBPIXEL) disp16[i] = (uint16_t)v16;
+        }
+    if (flags & SGMO_POST_MEDIAN) {
+        memcpy(dL, disp, N);
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                uint8_t v[9];
+                int k = 0;
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dx = -1; dx <= 1; dx++)
+                        v[k++] = dL[(size_t)clampi(y + dy, 0, H - 1) * W + clampi(x + dx, 0, W - 1)];
+                disp[(size_t)y * W + x] = median9(v);
+            }
+    }
+    rc = 0;
+out:
+    free(S); free(dL); free(dR);
+    return rc;
+}
+
 /* common/util.c:54-59 */
 uint64_t sgmo_fnv1a64(const void *data, size_t n)
 {

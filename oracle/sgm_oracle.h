@@ -13,6 +13,7 @@
  *   sgmo_gen_reference   common/gen_synthetic.c:21-112 (the reference's scene
  *                        generator, so its committed scenes can be rebuilt)
  *   sgmo_fnv1a64         common/util.c:54-59
+ *   sgmo_post            no reference counterpart (optional post-steps; see below)
  * D and the path count are runtime arguments here; the reference fixes them
  * at compile time (common/sgm_params.h:13-18), and the restatement is
  * checked against the reference's committed goldens at D = 64, 128, 256.
@@ -41,6 +42,17 @@ int sgmo_plain(const uint8_t *left, const uint8_t *right, int W, int H, int D, i
  * reference. disp is (W/2)*(H/2). W and H must be even (the reference reads
  * past its half-resolution cost volume otherwise). */
 int sgmo_multiscale(const uint8_t *left, const uint8_t *right, int W, int H, uint8_t *disp);
+
+/* Optional post-steps on the plain variant's summed volume (no reference
+ * counterpart: the reference has none, common/sgm_params.h:58); defined in
+ * sgm_oracle.c. flags: SGMO_POST_LR (left-right check, invalid = 255; D <=
+ * 240), SGMO_POST_MEDIAN (3x3 median after the check), SGMO_POST_SUBPIXEL
+ * (disp16 = 16 * d + parabola offset; 0xFFFF where the check failed). */
+#define SGMO_POST_LR       1
+#define SGMO_POST_MEDIAN   2
+#define SGMO_POST_SUBPIXEL 4
+int sgmo_post(const uint8_t *left, const uint8_t *right, int W, int H, int D, int paths, int flags,
+              uint8_t *disp, uint16_t *disp16);
 
 int sgmo_sobelx(const uint8_t *im, uint8_t *out, int W, int H);
 int sgmo_half(const uint8_t *im, uint8_t *out, int W, int H);

@@ -23,7 +23,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "
 CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wextra", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 
 CU_SOURCES = ["sgmgb_kernels.cu", "sgmgb_path.cu", "sgmgb_runtime.cu", "sgmgb_batch.cu", "sgmgb_server.cu",
-              "sgmgb_noalloc.cu", "sgmgb_sum.cu", "sgmgb_fused.cu"]
+              "sgmgb_noalloc.cu", "sgmgb_sum.cu", "sgmgb_fused.cu", "sgmgb_post.cu"]
 C_SOURCES = ["synth.c", "tune.c"]
 PLUGIN_VARIANTS = [(64, 4), (128, 4), (64, 8), (128, 8)]
 

@@ -53,6 +53,9 @@ struct sgmgb_ctx {
     const void *graph_key[kGraphs][3] = {};
     int graph_next = 0;
     PathShape shape;
+    // optional post-steps (sgmgb_run_frame_post): their workspace, made on first use
+    void *post = nullptr;
+    size_t post_bytes = 0;
 };
 
 // Device buffers of one frame slot. All pointers are carved from one

@@ -568,6 +568,7 @@ void sgmgb_destroy(sgmgb_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     drop_graph(ctx);
     slot_free(ctx->slot);
+    if (ctx->post) cudaFree(ctx->post);
     for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

@@ -20,6 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD, "libsgmgb.so")
 
 PLAIN, MULTISCALE = 0, 1
+POST_LR, POST_MEDIAN, POST_SUBPIXEL, DISP_INVALID = 1, 2, 4, 255
 SCHED_AUTO, SCHED_LATENCY, SCHED_THROUGHPUT, SCHED_FUSED, SCHED_SPLIT = 0, 1, 2, 3, 4
 OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_NODEV, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 
@@ -34,7 +35,7 @@ EXPORTS = [
     "sgmgb_batch_destroy", "sgmgb_tune_lookup", "sgmgb_tune_record",
     "sgmgb_server_create", "sgmgb_server_add_camera", "sgmgb_server_submit", "sgmgb_server_poll",
     "sgmgb_server_wait", "sgmgb_server_stats_get", "sgmgb_server_destroy", "sgmgb_synth_pair",
-    "sgmgb_server_prepare", "sgmgb_batch_busy",
+    "sgmgb_server_prepare", "sgmgb_batch_busy", "sgmgb_run_frame_post",
     "sgmgb_run_frame_noalloc",
 ]
 
@@ -95,6 +96,7 @@ def _load():
         "sgmgb_profile_frame": (i, [vp, u8p, u8p, u8p, i, ctypes.POINTER(KernelStat), i, ctypes.POINTER(i)]),
         "sgmgb_run_frame": (i, [vp, u8p, u8p, u8p, ctypes.POINTER(StageTimes)]),
         "sgmgb_run_frame_async": (i, [vp, u8p, u8p, u8p, vp]),
+        "sgmgb_run_frame_post": (i, [vp, u8p, u8p, u8p, vp, i]),
         "sgmgb_sync": (i, [vp, vp]),
         "sgmgb_census_async": (i, [vp, u8p, vp, i, i, vp]),
         "sgmgb_batch_create": (i, [vp, fdp, i, ctypes.c_char_p, ctypes.POINTER(vp)]),
@@ -274,6 +276,18 @@ class Engine:
         self._check(lib.sgmgb_run_frame(self.h, left.ctypes.data, right.ctypes.data, disp.ctypes.data,
                                         ctypes.byref(st)))
         return (disp, st.as_dict()) if times else disp
+
+    def run_frame_post(self, left, right, flags):
+        """The plain frame with optional post-steps (POST_LR, POST_MEDIAN,
+        POST_SUBPIXEL): (map, 16x subpixel map or None)."""
+        left = np.ascontiguousarray(left, np.uint8)
+        right = np.ascontiguousarray(right, np.uint8)
+        H, W = left.shape
+        disp = np.empty((H, W), np.uint8)
+        d16 = np.empty((H, W), np.uint16) if flags & POST_SUBPIXEL else None
+        self._check(lib.sgmgb_run_frame_post(self.h, left.ctypes.data, right.ctypes.data, disp.ctypes.data,
+                                             d16.ctypes.data if d16 is not None else None, flags))
+        return disp, d16
 
     def run_frame_async(self, d_left, d_right, d_disp, stream=None):
         """Device buffers (torch tensors or addresses), enqueued on `stream`."""
