@@ -94,9 +94,9 @@ def test_post_steps_reject(engine):
     engine.plan(64, 32, 64, 4)
     with pytest.raises(sgmgb.SgmError):
         engine.run_frame_post(left, right, 8)
-    with pytest.raises(sgmgb.SgmError):
-        sgmgb.lib.sgmgb_run_frame_post(engine.h, left.ctypes.data, right.ctypes.data,
-                                       np.empty_like(left).ctypes.data, None, sgmgb.POST_SUBPIXEL)
+    assert sgmgb.lib.sgmgb_run_frame_post(engine.h, left.ctypes.data, right.ctypes.data,
+                                          np.empty_like(left).ctypes.data, None,
+                                          sgmgb.POST_SUBPIXEL) == sgmgb.ERR_ARG   # no subpixel buffer
     engine.plan(64, 32, 64, 8, sgmgb.MULTISCALE)
     with pytest.raises(sgmgb.SgmError):
         engine.run_frame_post(left, right, 0)
