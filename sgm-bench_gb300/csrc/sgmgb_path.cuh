@@ -393,8 +393,12 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
             if (i0 < glim[j]) {
                 const uint32_t db = dst + (uint32_t)((lane + 32 * j) * 16);
                 cp_async16(db, P.C + goff[j]);
+                // even-only finals: the planes hold values at even (x, y) only, and only
+                // those pixels' argmins are kept, so the other granules' planes are not read
+                if (ost[j]) {
 #pragma unroll
-                for (int q = 0; q < NPL; q++) cp_async16(db + (uint32_t)((1 + q) * K * SBM), pl[q] + goff[j]);
+                    for (int q = 0; q < NPL; q++) cp_async16(db + (uint32_t)((1 + q) * K * SBM), pl[q] + goff[j]);
+                }
             }
             goff[j] += adv;
         }
