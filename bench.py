@@ -499,6 +499,47 @@ def reference_checker(Dk, paths):
     return (lambda l, r: oracle.plain(l, r, Dk, paths)), "port"
 
 
+def reference_gpu_section(left, right):
+    """The reference's own CUDA programs, built for sm_103a from its sources
+    by oracle/build_ref.sh and run on this GPU: cuda/sgm_cuda_opt.cu (4 paths,
+    D = 64 and 128) in the reference's harness, timed by the harness on its
+    pageable buffers (cuda/sgm_cuda_opt.cu:321-366 copies them in and out
+    inside each run), and multiscale/sgm_ms_cuda.cu on configurations B and C
+    (its own main and timing, multiscale/sgm_ms_cuda.cu:160-208). A same-GPU
+    comparison, not the target. Each map is compared with the reference's CPU
+    program on the same pair."""
+    import oracle
+    out = {"what": "the reference's CUDA programs built for sm_103a (oracle/build_ref.sh), same GPU"}
+    if not os.path.exists("/dev/nvidiactl"):
+        out["unavailable"] = "no GPU on this host"
+        return out
+    for Dk in (64, 128):
+        name = "cuda_opt_d%d_1920x1080" % Dk
+        try:
+            t, disp = oracle.reference_cuda_plain(left, right, Dk)
+            want, _ = reference_checker(Dk, 4)
+            t["equal_to_reference_cpu"] = bool(np.array_equal(disp, want(left, right)))
+            t["mde_per_s"] = W * H * Dk / (t["median_ms"] / 1e3) / 1e6
+            t["call"] = ("common/harness.c: median of %d runs after %d warm-up, each run copies the pageable "
+                         "images in and the map out" % (t["runs"], t["warmup"]))
+            out[name] = t
+        except Exception as e:                      # not built, or it failed: say so, keep the line
+            out[name] = {"unavailable": (str(e).strip().splitlines() or ["?"])[0][:200]}
+    for name, (Wm, Hm) in (("ms_cuda_configB_1920x800", (1920, 800)), ("ms_cuda_configC_1920x1080", (1920, 1080))):
+        try:
+            l2, r2, _ = oracle.synth_pair(Wm, Hm, 64, 300)
+            ms, h, _ = oracle.reference_cuda_multiscale(l2, r2)
+            _, h_cpu, _, _ = oracle.reference_multiscale(l2, r2, reps=1)
+            work = ((Wm // 2) * (Hm // 2) + Wm * Hm) * 64
+            out[name] = {"median_ms": ms, "hash": h, "equal_to_reference_cpu": h == h_cpu,
+                         "mde_per_s_work": work / (ms / 1e3) / 1e6,
+                         "call": "its own main: inputs copied once, each timed frame the kernels and the map "
+                                 "copied out, median of 10 after 3 warm-up"}
+        except Exception as e:
+            out[name] = {"unavailable": (str(e).strip().splitlines() or ["?"])[0][:200]}
+    return out
+
+
 def run_reference(args):
     """The reference's CPU implementation of the path (common/sgm_ref.c through
     its SGM_IMPL, built from its sources by oracle/build_ref.sh; the oracle port
@@ -540,6 +581,8 @@ def run_reference(args):
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not getattr(args, "no_refgpu", False):
+        line["reference_gpu"] = reference_gpu_section(*pairs[0])
     print(json.dumps(line))
     return 0
 
@@ -798,6 +841,8 @@ def main():
     ap.add_argument("--no-multiscale", action="store_true", help="skip the configurations B/C section")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-form section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the D x resolution grid")
+    ap.add_argument("--no-refgpu", action="store_true",
+                    help="reference arm: skip the reference's own CUDA programs on this GPU")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -224,3 +224,62 @@ def reference_multiscale(left, right, reps=1, threads=None):
     if p.returncode != 0 or not m:
         raise RuntimeError("sgm_ms_ref failed: " + p.stdout + p.stderr)
     return float(m.group(1)), m.group(2), omp, threads
+
+
+# ---- the reference's own CUDA programs (built by build_ref.sh where nvcc is present) ----
+def _read_pgm(path):
+    with open(path, "rb") as f:
+        data = f.read()
+    m = re.match(rb"P5\s+(\d+)\s+(\d+)\s+(\d+)\s", data)
+    if not m:
+        raise ValueError("not a binary PGM: %s" % path)
+    W, H = int(m.group(1)), int(m.group(2))
+    return np.frombuffer(data[m.end():m.end() + W * H], np.uint8).reshape(H, W).copy()
+
+
+def reference_cuda_available(what="sgm_cuda_opt_d64"):
+    return os.path.exists(os.path.join(REF_DIR, what))
+
+
+def reference_cuda_plain(left, right, D=64, warm=3, timed=20, timeout=120):
+    """Runs the reference's cuda/sgm_cuda_opt.cu (4 paths, compile-time D) in
+    the reference's own harness (common/harness.c) on this pair, with the
+    harness's cost gate off. Each timed run is the harness's call: its
+    pageable buffers copied in, the kernels, the map copied out. Returns
+    (dict of the harness's median / p95 / min in ms, the map)."""
+    exe = os.path.join(REF_DIR, "sgm_cuda_opt_d%d" % D)
+    if not os.path.exists(exe):
+        raise FileNotFoundError("reference CUDA program not built: %s (oracle/build_ref.sh)" % exe)
+    with tempfile.TemporaryDirectory() as d:
+        lp, rp, op = (os.path.join(d, n) for n in ("l.pgm", "r.pgm", "o.pgm"))
+        write_pgm(lp, left)
+        write_pgm(rp, right)
+        p = subprocess.run([exe, lp, rp, "-o", op, "-w", str(warm), "-n", str(timed), "--no-roofline"],
+                           capture_output=True, text=True, timeout=timeout)
+        m = re.search(r"median\s+([0-9.]+) ms\s+p95\s+([0-9.]+)\s+min\s+([0-9.]+).* hash ([0-9a-f]{16})", p.stdout)
+        if p.returncode != 0 or not m:
+            raise RuntimeError("sgm_cuda_opt failed: " + p.stdout + p.stderr)
+        disp = _read_pgm(op)
+    return {"median_ms": float(m.group(1)), "p95_ms": float(m.group(2)), "min_ms": float(m.group(3)),
+            "hash": m.group(4), "runs": timed, "warmup": warm}, disp
+
+
+def reference_cuda_multiscale(left, right, reps=10, timeout=120):
+    """Runs the reference's multiscale/sgm_ms_cuda.cu on this pair (its own
+    main: the inputs copied once, then per timed frame the kernels and the
+    map copied out; 3 warm-up frames). Returns (median ms it prints, its FNV
+    hash, the half-resolution map)."""
+    exe = os.path.join(REF_DIR, "sgm_ms_cuda")
+    if not os.path.exists(exe):
+        raise FileNotFoundError("reference multi-scale CUDA program not built (oracle/build_ref.sh)")
+    with tempfile.TemporaryDirectory() as d:
+        lp, rp, op = (os.path.join(d, n) for n in ("l.pgm", "r.pgm", "o.pgm"))
+        write_pgm(lp, left)
+        write_pgm(rp, right)
+        p = subprocess.run([exe, lp, rp, "-o", op, "-n", str(reps)], capture_output=True, text=True,
+                           timeout=timeout)
+        m = re.search(r"median ([0-9.]+) ms .* hash ([0-9a-f]{16})", p.stdout)
+        if p.returncode != 0 or not m:
+            raise RuntimeError("sgm_ms_cuda failed: " + p.stdout + p.stderr)
+        disp = _read_pgm(op)
+    return float(m.group(1)), m.group(2), disp

@@ -88,3 +88,4 @@ def test_reference_arm_line_matches_the_gpu_arm_config(monkeypatch):
     assert line["cpu_baseline"]["kind"] in ("reference", "port")
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    assert "what" in line["reference_gpu"]             # the reference's CUDA programs, or why not
