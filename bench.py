@@ -58,6 +58,12 @@ B_ALG = 2 * W * H * D + 3 * W * H          # modelled minimal bytes per frame
 KERNELS_PER_FRAME = 2 + PATHS               # census + cost volume + one pass per direction
 
 
+def alone_sched(sgmgb):
+    """The schedule SGMGB_SCHED_AUTO gives a frame of this workload that has
+    the GPU to itself (the synchronous call): SPLIT from 2 Mpixel at D >= 64."""
+    return sgmgb.SCHED_SPLIT if W * H >= 2000000 and D >= 64 and PATHS == 4 else sgmgb.SCHED_LATENCY
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -634,9 +640,10 @@ def run_gb300(args):
         for i in range(n):
             engines[i % nf].run_frame_async(dl[i % R], dr[i % R], dd[i % R], stream=streams[i % nf])
 
-    # one frame at a time (a single context and stream, the latency schedule),
-    # for the frame latency
-    eng.set_schedule(sgmgb.SCHED_LATENCY)
+    # one frame at a time (a single context and stream), for the frame latency,
+    # with the schedule the synchronous call takes under AUTO for a frame alone
+    # of this size (SPLIT: at least 2 Mpixel at D >= 64)
+    eng.set_schedule(alone_sched(sgmgb))
     run_frames(3, 1)
     torch.cuda.synchronize(dev)
     e0s, e1s = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -720,10 +727,10 @@ def run_gb300(args):
     pg_exact = bool(np.array_equal(plug.run(pl[0], pr[0])[1], maps0[0]))
 
     # per-kernel device time, each kernel alone, CUDA events on the engine's
-    # stream: the fused schedule (`value`) and the latency one (`e2e`)
+    # stream: the fused schedule (`value`) and the one of a frame alone (`e2e`)
     eng.set_schedule(sgmgb.SCHED_FUSED)
     kstats = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
-    eng.set_schedule(sgmgb.SCHED_LATENCY)
+    eng.set_schedule(alone_sched(sgmgb))
     kstats_lat = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
     eng.set_schedule(sgmgb.SCHED_AUTO)
 
@@ -757,9 +764,9 @@ def run_gb300(args):
                 "fps": ws * e2e_steps / e2e_s, "p50_ms": statistics.median(lat) * 1e3,
                 "p99_ms": sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
                 "stage_ms": {k: round(v, 4) for k, v in st.items() if k.endswith("_ms")},
-                "schedule": "latency (one frame at a time)",
-                "transfers": "pinned host buffers: the first kernel reads both images and the sum pass writes the "
-                             "map across NVLink-C2C inside the call",
+                "schedule": "split (auto for one 1920x1080 D=64 frame at a time)",
+                "transfers": "pinned host buffers: the census kernel reads both images across NVLink-C2C inside "
+                             "the call; the map comes back with one copy",
                 "same_map_as_device_path": e2e_exact,
                 "pageable": {"value": replica_value(ws, e2e_steps, pg_s), "unit": UNIT,
                              "fps": ws * e2e_steps / pg_s, "p50_ms": statistics.median(lat_pg) * 1e3,

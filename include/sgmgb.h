@@ -114,10 +114,12 @@ int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane
  *               first halves of the rows run side by side with the vertical
  *               directions: the shortest critical path of the four. Same
  *               frames as FUSED; other frames run THROUGHPUT;
- *   AUTO        LATENCY for sgmgb_run_frame and for a server frame with
- *               nothing else in flight, FUSED (THROUGHPUT where FUSED does not
- *               apply) for sgmgb_run_frame_async and the other server frames
- *               (the default).
+ *   AUTO        for sgmgb_run_frame and for a server frame with nothing
+ *               else in flight: SPLIT on frames of at least 2,000,000 pixels
+ *               at D >= 64 where it applies, LATENCY on the others; FUSED
+ *               (THROUGHPUT where FUSED does not apply) for
+ *               sgmgb_run_frame_async and the other server frames (the
+ *               default).
  * Drops cached graphs. */
 #define SGMGB_SCHED_AUTO       0
 #define SGMGB_SCHED_LATENCY    1
@@ -131,7 +133,8 @@ int  sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule);
  * W*H bytes, row-major; disp receives the output map (sgmgb_out_size).
  * Page-locked (or CUDA-registered) buffers are read and written across
  * NVLink-C2C by the kernels themselves; other host memory goes through the
- * copy engines. Runs the latency schedule under SGMGB_SCHED_AUTO. */
+ * copy engines. Under SGMGB_SCHED_AUTO it runs the schedule of a frame that
+ * has the GPU to itself (SPLIT or LATENCY, above). */
 int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right,
                     uint8_t *disp, sgmgb_stage_times *t);
 /* Device buffers, enqueued on `stream` (a cudaStream_t, NULL = the context's

@@ -16,23 +16,28 @@ struct PathShape {
     int sched = SGMGB_SCHED_AUTO;
 };
 
-// The schedule a frame runs with. AUTO becomes LATENCY for a frame that has
-// the GPU to itself (the synchronous host-buffer call, a server frame with
-// nothing else in flight) and FUSED otherwise, which runs THROUGHPUT for the
-// frames it does not cover (fused_applies). Measured with four 1920x1080
-// frames in flight: FUSED 0.242 ms per frame at D = 64 against 0.259 for
-// THROUGHPUT (0.486 against 0.510 at D = 128, 0.184 against 0.197 at D = 32);
-// a frame alone: LATENCY 0.340 ms at D = 64 against 0.363 for FUSED.
-inline PathShape resolve_sched(PathShape s, bool alone) {
-    if (s.sched == SGMGB_SCHED_AUTO) s.sched = alone ? SGMGB_SCHED_LATENCY : SGMGB_SCHED_FUSED;
-    return s;
-}
-
 // The fused schedule covers the plain variant with 4 paths in the
 // two-lines-per-warp layout (D = 32, 64 or 128, no disparities-per-lane
 // shape); other frames asking for it run the throughput schedule.
 inline bool fused_applies(const sgmgb_frame_desc &fd, const PathShape &s) {
     return fd.variant == SGMGB_PLAIN && fd.paths == 4 && s.dpl == 0 && (fd.D == 32 || fd.D == 64 || fd.D == 128);
+}
+
+// The schedule a frame runs with. AUTO becomes FUSED (THROUGHPUT for the
+// frames it does not cover) when frames share the GPU, and for a frame that
+// has the GPU to itself (the synchronous host-buffer call, a server frame
+// with nothing else in flight) SPLIT on frames of at least 2 Mpixel at
+// D >= 64, LATENCY on the others. Measured on 1920x1080 frames, ms per frame
+// with four in flight, FUSED / THROUGHPUT: D=64 0.251 / 0.259, D=128
+// 0.480 / 0.512, D=32 0.185 / 0.197; a frame alone, SPLIT / LATENCY: D=64
+// 0.327 / 0.340, D=128 0.639 / 0.697, D=32 0.254 / 0.237, and 1280x720
+// D=128 0.374 / 0.329.
+inline PathShape resolve_sched(PathShape s, bool alone, const sgmgb_frame_desc &fd) {
+    if (s.sched != SGMGB_SCHED_AUTO) return s;
+    if (!alone) s.sched = SGMGB_SCHED_FUSED;
+    else s.sched = fused_applies(fd, s) && (size_t)fd.W * fd.H >= 2000000 && fd.D >= 64 ? SGMGB_SCHED_SPLIT
+                                                                                         : SGMGB_SCHED_LATENCY;
+    return s;
 }
 
 struct sgmgb_ctx {

@@ -236,7 +236,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     pa -= step; pb -= step; xa -= dx; ya -= dy; xb -= dx; yb -= dy;
     const int hw = P.W >> 1;
 
-    uint32_t dacc[2][KW];                             // FINAL3H: the chunk's disparities of rows A and B, byte k = step k
+    uint32_t dacc[2][KW] = {};                        // FINAL3H: the chunk's disparities of rows A and B, byte k = step k
     // one step of both lines; `row`: this step's cost row in the chunk; kk: the step within the chunk
     auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&ps)[NR], const uint32_t (&sv)[NR], uint8_t *row,
                          int i, int kk, auto full_t) {
@@ -298,6 +298,21 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             return;
         }
         // final passes: argmin over d, the lowest d winning ties; every lane reaches the reductions
+        if (MODE == MODE_FINAL3H && KEY16) {
+            // gather the chunk's disparities per row: byte kk & 3 of word kk >> 2 takes the low
+            // byte of line A's minimal key (d in its low 6 bits) and byte 2 of the packed
+            // minimum (line B's key in the high half); the words are masked to 6-bit bytes
+            // when the chunk is stored
+            uint32_t k = tot[0] * 64u + dpk[0];                    // S*64 + d (S <= 1016)
+#pragma unroll
+            for (int j = 1; j < NR; j++) k = vmin2(k, tot[j] * 64u + dpk[j]);
+            const uint32_t ra = __reduce_min_sync(kFull, k & 0xFFFFu);
+            const uint32_t rb = __reduce_min_sync(kFull, k);
+            const int q = kk & 3, wq = kk >> 2;
+            dacc[0][wq] = q == 0 ? ra : __byte_perm(dacc[0][wq], ra, q == 1 ? 0x3240 : (q == 2 ? 0x3410 : 0x4210));
+            dacc[1][wq] = __byte_perm(q == 0 ? rb : dacc[1][wq], rb, q == 0 ? 0x0002 : (q == 1 ? 0x3260 : (q == 2 ? 0x3610 : 0x6210)));
+            return;
+        }
         uint32_t da, db;
         if (KEY16) {
             uint32_t k = kFull;
@@ -367,7 +382,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             }
         }
         const long long pa0 = pa + step, pb0 = pb + step;   // the chunk's first pixel of each line
-        if (MODE == MODE_FINAL3H) {
+        if (MODE == MODE_FINAL3H && !KEY16) {
 #pragma unroll
             for (int w = 0; w < KW; w++) dacc[0][w] = dacc[1][w] = 0u;
         }
@@ -387,14 +402,16 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
                 if (n <= 0) continue;
                 const long long p0 = r ? pb0 : pa0;
                 const long long lo = dx > 0 ? p0 : p0 - (K - 1);     // lowest address of a whole chunk
+                constexpr uint32_t dm = KEY16 ? 0x3F3F3F3Fu : 0xFFFFFFFFu;
                 if (n == K && K % 4 == 0 && (((uintptr_t)(P.disp + lo)) & 3) == 0) {
 #pragma unroll
                     for (int w = 0; w < KW; w++)
-                        ((uint32_t *)(P.disp + lo))[w] = dx > 0 ? dacc[r][w] : __byte_perm(dacc[r][KW - 1 - w], 0, 0x0123);
+                        ((uint32_t *)(P.disp + lo))[w] =
+                            dm & (dx > 0 ? dacc[r][w] : __byte_perm(dacc[r][KW - 1 - w], 0, 0x0123));
                 } else {
 #pragma unroll
                     for (int k = 0; k < K; k++)
-                        if (k < n) P.disp[p0 + dx * k] = (uint8_t)(dacc[r][k >> 2] >> (8 * (k & 3)));
+                        if (k < n) P.disp[p0 + dx * k] = (uint8_t)((dacc[r][k >> 2] >> (8 * (k & 3))) & dm);
                 }
             }
         }

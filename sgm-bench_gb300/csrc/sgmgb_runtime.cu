@@ -514,7 +514,7 @@ int sgmgb_profile_frame(sgmgb_ctx *ctx, const uint8_t *d_left, const uint8_t *d_
     int n = 0;
     for (int r = 0; r < reps && e == cudaSuccess; r++) {
         pr.n = 0;
-        e = enqueue_frame(*ctx->slot, d_left, d_right, d_disp, ctx->stream, resolve_sched(ctx->shape, true),
+        e = enqueue_frame(*ctx->slot, d_left, d_right, d_disp, ctx->stream, resolve_sched(ctx->shape, true, ctx->fd),
                           nullptr, nullptr, &pr);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         for (int k = 0; k < pr.n && e == cudaSuccess; k++) {
@@ -638,17 +638,19 @@ int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right, u
     const size_t outN = (size_t)ow * oh;
     // Page-locked (or registered) host buffers cross NVLink-C2C inside the
     // kernels: a plain frame's census reads the images from host memory (its
-    // 32-row tiles stage them with 16-byte loads) and the sum pass of the
-    // latency schedule writes the map into it, so the transfers overlap the
-    // compute. Other host buffers, and the multi-scale images (read byte by
+    // 32-row tiles stage them with 16-byte loads) and the last passes of the
+    // latency and split schedules write the map into it, so the transfers
+    // overlap the compute (the other schedules copy the map back). Other host buffers, and the multi-scale images (read byte by
     // byte by its prefilters), go through the copy engines. (Measured slower:
     // the two images on two streams; the images in two row bands with the
     // census of the top band started early.) One stream, one wait at the end.
     cudaStream_t st = ctx->stream;
-    const PathShape shape = resolve_sched(ctx->shape, true);
+    const PathShape shape = resolve_sched(ctx->shape, true, ctx->fd);
     const bool plain = s.fd.variant == SGMGB_PLAIN;
     const uint8_t *hl = plain ? host_view(left) : nullptr, *hr = plain ? host_view(right) : nullptr;
-    uint8_t *hd = shape.sched == SGMGB_SCHED_LATENCY ? (uint8_t *)host_view(disp) : nullptr;
+    const bool map_direct = shape.sched == SGMGB_SCHED_LATENCY ||
+                            (shape.sched == SGMGB_SCHED_SPLIT && fused_applies(s.fd, shape));
+    uint8_t *hd = map_direct ? (uint8_t *)host_view(disp) : nullptr;
     cudaEvent_t *ev = ctx->ev;   // 0 start, 3 inputs in, 1 census and cost done, 2 frame done, 4 map out
     cudaError_t e = cudaEventRecord(ev[0], st);
     if (e == cudaSuccess && !hl) e = cudaMemcpyAsync(s.left, left, N, cudaMemcpyHostToDevice, st);
@@ -692,7 +694,7 @@ static cudaError_t capture_frame_graph(sgmgb_ctx *ctx, const uint8_t *l, const u
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    cudaError_t ee = enqueue_frame(*ctx->slot, l, r, d, ctx->stream, resolve_sched(ctx->shape, false), nullptr,
+    cudaError_t ee = enqueue_frame(*ctx->slot, l, r, d, ctx->stream, resolve_sched(ctx->shape, false, ctx->fd), nullptr,
                                    nullptr);
     e = cudaStreamEndCapture(ctx->stream, &g);
     if (ee != cudaSuccess) { if (g) cudaGraphDestroy(g); return ee; }

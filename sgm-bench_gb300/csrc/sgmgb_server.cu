@@ -136,8 +136,8 @@ bool make_slot(const sgmgb_frame_desc &fd, Slot *out) {
 }
 
 // Enqueues request r on slot k of its camera (no lock held). `alone`: the
-// frame was admitted with nothing else in flight (the latency schedule under
-// SGMGB_SCHED_AUTO).
+// frame was admitted with nothing else in flight (under SGMGB_SCHED_AUTO the
+// schedule of a frame alone: SPLIT or LATENCY by size).
 bool launch(sgmgb_server *s, Request *r, int k, bool alone, std::string &err) {
     Camera *c = r->cam;
     Slot &sl = c->slots[k];
@@ -146,7 +146,7 @@ bool launch(sgmgb_server *s, Request *r, int k, bool alone, std::string &err) {
     cudaError_t e = cudaMemcpyAsync(fs.left, hb, c->n_in, cudaMemcpyHostToDevice, sl.st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fs.right, hb + c->n_in, c->n_in, cudaMemcpyHostToDevice, sl.st);
     if (e == cudaSuccess)
-        e = enqueue_frame(fs, fs.left, fs.right, fs.disp, sl.st, resolve_sched(s->ctx->shape, alone), nullptr, nullptr);
+        e = enqueue_frame(fs, fs.left, fs.right, fs.disp, sl.st, resolve_sched(s->ctx->shape, alone, fs.fd), nullptr, nullptr);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hb + 2 * c->n_in, fs.disp, c->n_out, cudaMemcpyDeviceToHost, sl.st);
     if (e == cudaSuccess) e = cudaLaunchHostFunc(sl.st, on_frame_done, r);
     if (e != cudaSuccess) {

@@ -236,6 +236,34 @@ def test_profile_frame_lists_every_kernel(engine):
         engine.set_schedule(sgmgb.SCHED_AUTO)
 
 
+def test_auto_runs_split_for_a_large_frame_alone(engine):
+    """Under AUTO a frame alone of at least 2 Mpixel at D >= 64 takes the split
+    schedule (the profile lists its kernels), and the synchronous call, whose
+    last passes write the map straight into page-locked host memory, returns
+    the checker's map."""
+    import torch
+    from conftest import reference_plain
+    W, H, D = 1920, 1080, 64
+    left, right, _ = sgmgb.synth_pair(W, H, D, seed=11)
+    want = reference_plain(left, right, D, 4)
+    engine.set_schedule(sgmgb.SCHED_AUTO)
+    engine.plan(W, H, D, 4)
+    dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
+    dd = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+    names = [s[0] for s in engine.profile_frame(dl, dr, dd, reps=1)]
+    assert names == ["census", "cost", "path_tb", "path_bt", "path_lr_first", "path_rl_first", "path_lr_final",
+                     "path_rl_final"]
+    assert np.array_equal(dd.cpu().numpy(), want)
+    hl = torch.from_numpy(left).pin_memory().numpy()
+    hr = torch.from_numpy(right).pin_memory().numpy()
+    ho = torch.zeros((H, W), dtype=torch.uint8).pin_memory().numpy()
+    for _ in range(2):
+        engine.run_frame(hl, hr, out=ho)
+        assert np.array_equal(ho, want)
+        ho[:] = 0
+    assert np.array_equal(engine.run_frame(left, right), want)         # pageable: through the copy engines
+
+
 SCHEDS = {"latency": sgmgb.SCHED_LATENCY, "throughput": sgmgb.SCHED_THROUGHPUT, "fused": sgmgb.SCHED_FUSED,
           "split": sgmgb.SCHED_SPLIT}
 
