@@ -83,10 +83,16 @@ struct FrameSlot {
     uint8_t *hsobL = nullptr, *hsobR = nullptr;                   // half-scale SobelX
     uint64_t *cl1 = nullptr, *cr1 = nullptr;                      // half-scale census
     uint8_t *disp1 = nullptr;                                     // stage-1 argmin (defined work, unused)
+    uint8_t *P1 = nullptr;                                        // the half-scale stage's 8 direction planes
     // independent path passes of one frame run on forked streams
     static constexpr int kAux = 7;
     cudaStream_t aux[kAux] = {};
     cudaEvent_t fork = nullptr, join[kAux] = {};
+    // multi-scale: the half-scale stage runs on a stream set of its own beside
+    // the full-scale one (ms, aux2, fork2, join2); fork_ms hands it the inputs,
+    // c1 marks its cost volume (the full-scale cost merge reads it), s1_done its end
+    cudaStream_t ms = nullptr, aux2[kAux] = {};
+    cudaEvent_t fork2 = nullptr, join2[kAux] = {}, fork_ms = nullptr, c1 = nullptr, s1_done = nullptr;
 };
 
 namespace sgmgb {

@@ -30,7 +30,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
     const size_t o_xp = take(N * D * (fd.paths == 8 ? 5 : 1));
     const size_t o_state = fd.variant == SGMGB_PLAIN ? take(hstate_words(fd.H) * 4) : 0;
     size_t o_sobL = 0, o_sobR = 0, o_hL = 0, o_hR = 0, o_hsL = 0, o_hsR = 0, o_cl1 = 0, o_cr1 = 0, o_d1 = 0;
-    size_t o_C1 = 0;
+    size_t o_C1 = 0, o_P1 = 0;
     if (fd.variant == SGMGB_MULTISCALE) {
         const size_t Nh = (W / 2) * (H / 2);
         o_sobL = take(N); o_sobR = take(N);
@@ -38,6 +38,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
         o_cl1 = take(Nh * 8); o_cr1 = take(Nh * 8);
         o_d1 = take(Nh);
         o_C1 = take(Nh * D);
+        o_P1 = take(Nh * D * 8);
     }
     if (s) {
         uint8_t *b = (uint8_t *)s->base;
@@ -52,6 +53,7 @@ size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s) {
             s->halfL = b + o_hL; s->halfR = b + o_hR; s->hsobL = b + o_hsL; s->hsobR = b + o_hsR;
             s->cl1 = (uint64_t *)(b + o_cl1); s->cr1 = (uint64_t *)(b + o_cr1);
             s->disp1 = b + o_d1;
+            s->P1 = b + o_P1;
         }
     }
     return off;
@@ -75,6 +77,15 @@ int slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
     for (int i = 0; i < FrameSlot::kAux && e == cudaSuccess; i++)
         e = cudaEventCreateWithFlags(&s->join[i], cudaEventDisableTiming);
+    if (fd.variant == SGMGB_MULTISCALE) {
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->ms, cudaStreamNonBlocking);
+        for (int i = 0; i < FrameSlot::kAux && e == cudaSuccess; i++)
+            e = cudaStreamCreateWithFlags(&s->aux2[i], cudaStreamNonBlocking);
+        for (cudaEvent_t *ev : {&s->fork2, &s->fork_ms, &s->c1, &s->s1_done})
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        for (int i = 0; i < FrameSlot::kAux && e == cudaSuccess; i++)
+            e = cudaEventCreateWithFlags(&s->join2[i], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
         err = std::string("stream/event creation: ") + cudaGetErrorString(e);
         cudaGetLastError();
@@ -88,8 +99,11 @@ int slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err) {
 void slot_free(FrameSlot *s) {
     if (!s) return;
     for (auto &a : s->aux) if (a) cudaStreamDestroy(a);
-    if (s->fork) cudaEventDestroy(s->fork);
+    for (auto &a : s->aux2) if (a) cudaStreamDestroy(a);
+    if (s->ms) cudaStreamDestroy(s->ms);
+    for (cudaEvent_t ev : {s->fork, s->fork2, s->fork_ms, s->c1, s->s1_done}) if (ev) cudaEventDestroy(ev);
     for (auto &j : s->join) if (j) cudaEventDestroy(j);
+    for (auto &j : s->join2) if (j) cudaEventDestroy(j);
     if (s->base) cudaFree(s->base);
     delete s;
 }
@@ -134,22 +148,43 @@ const char *pass_name(int dx, int dy) {
 // (MODE_FINAL3 for 4 paths, MODE_FINAL7 for 8). One plane less is written
 // and read than with run_planes, at the price of a long pass on the frame's
 // critical path.
-cudaError_t run_final(const FrameSlot &s, const LineParams &base, int npaths, int sat, bool ms, int wpb,
+// The forked streams, events and direction planes of one group of path
+// passes: the frame's own (main_fan), or, for the half-scale stage of a
+// multi-scale frame, which runs beside the full-scale stage, a set of its own
+// (half_fan). `plane`: bytes of one direction's plane at the group's scale.
+struct Fan {
+    const cudaStream_t *aux;
+    cudaEvent_t fork;
+    const cudaEvent_t *join;
+    uint8_t *pl[8];
+};
+
+Fan main_fan(const FrameSlot &s, size_t plane) {
+    return Fan{s.aux, s.fork, s.join, {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane, s.xp, s.xp + plane,
+                                       s.xp + 2 * plane, s.xp + 3 * plane, s.xp + 4 * plane}};
+}
+
+Fan half_fan(const FrameSlot &s, size_t plane) {
+    Fan f{s.aux2, s.fork2, s.join2, {}};
+    for (int k = 0; k < 8; k++) f.pl[k] = s.P1 + k * plane;
+    return f;
+}
+
+cudaError_t run_final(const Fan &f, const LineParams &base, int npaths, int sat, bool ms, int wpb,
                       cudaStream_t st, Marker &mark, int even_only, uint8_t *disp, double Nout) {
     const bool serial = mark.pr != nullptr;
     const size_t plane = (size_t)base.W * base.H * base.D;
-    uint8_t *pl[7] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane, s.xp, s.xp + plane, s.xp + 2 * plane,
-                      s.xp + 3 * plane};
+    uint8_t *const *pl = f.pl;
     static const int dirs[7][2] = {{-1, 0}, {1, 0}, {0, -1}, {-1, -1}, {1, 1}, {1, -1}, {-1, 1}};
     const int nsc = npaths - 1;
     const double ND = (double)plane;
     cudaStream_t ss[7];
-    for (int k = 0; k < nsc; k++) ss[k] = (serial || k == 0) ? st : s.aux[k - 1];
+    for (int k = 0; k < nsc; k++) ss[k] = (serial || k == 0) ? st : f.aux[k - 1];
     cudaError_t e;
     if (!serial) {
-        if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(f.fork, st)) != cudaSuccess) return e;
         for (int k = 1; k < nsc; k++)
-            if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(ss[k], f.fork, 0)) != cudaSuccess) return e;
     }
     for (int k = 0; k < nsc; k++) {
         LineParams q = base;
@@ -161,8 +196,8 @@ cudaError_t run_final(const FrameSlot &s, const LineParams &base, int npaths, in
     }
     if (!serial) {
         for (int k = 1; k < nsc; k++) {
-            if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(f.join[k - 1], ss[k])) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(st, f.join[k - 1], 0)) != cudaSuccess) return e;
         }
     }
     LineParams q = base;
@@ -184,21 +219,20 @@ cudaError_t run_final(const FrameSlot &s, const LineParams &base, int npaths, in
 // one pass then adds the planes and takes the argmin into `disp` (even_only:
 // the multi-scale full scale's (W/2)x(H/2) map). `serial` (a probe
 // attached): all on `st`, one after another.
-cudaError_t run_planes(const FrameSlot &s, const LineParams &base, int npaths, int sat, bool ms, int wpb,
+cudaError_t run_planes(const Fan &f, const LineParams &base, int npaths, int sat, bool ms, int wpb,
                        cudaStream_t st, Marker &mark, int even_only, uint8_t *disp, double Nout) {
     const bool serial = mark.pr != nullptr;
-    const size_t plane = (size_t)base.W * base.H * base.D;   // at this scale (fits the full-scale buffers)
-    uint8_t *pl[8] = {s.sc, (uint8_t *)s.S, (uint8_t *)s.S + plane, s.xp, s.xp + plane, s.xp + 2 * plane,
-                      s.xp + 3 * plane, s.xp + 4 * plane};
+    const size_t plane = (size_t)base.W * base.H * base.D;   // at this scale (fits the fan's buffers)
+    uint8_t *const *pl = f.pl;
     static const int dirs[8][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}, {-1, -1}, {1, 1}, {1, -1}, {-1, 1}};
     const double ND = (double)plane;
     cudaStream_t ss[8];
-    for (int k = 0; k < npaths; k++) ss[k] = (serial || k == 0) ? st : s.aux[k - 1];
+    for (int k = 0; k < npaths; k++) ss[k] = (serial || k == 0) ? st : f.aux[k - 1];
     cudaError_t e;
     if (!serial) {
-        if ((e = cudaEventRecord(s.fork, st)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(f.fork, st)) != cudaSuccess) return e;
         for (int k = 1; k < npaths; k++)
-            if ((e = cudaStreamWaitEvent(ss[k], s.fork, 0)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(ss[k], f.fork, 0)) != cudaSuccess) return e;
     }
     SumPlanes sp{};
     for (int k = 0; k < npaths; k++) {
@@ -212,8 +246,8 @@ cudaError_t run_planes(const FrameSlot &s, const LineParams &base, int npaths, i
     }
     if (!serial) {
         for (int k = 1; k < npaths; k++) {
-            if ((e = cudaEventRecord(s.join[k - 1], ss[k])) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(st, s.join[k - 1], 0)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(f.join[k - 1], ss[k])) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(st, f.join[k - 1], 0)) != cudaSuccess) return e;
         }
     }
     if ((e = launch_sum(sp, npaths, disp, base.W, base.H, base.D, even_only, st)) != cudaSuccess) return e;
@@ -338,11 +372,11 @@ cudaError_t run_split(const FrameSlot &s, const LineParams &base, int wpb, cudaS
     return cudaSuccess;
 }
 
-cudaError_t run_dirs(const PathShape &shape, const FrameSlot &s, const LineParams &base, int npaths, int sat,
+cudaError_t run_dirs(const PathShape &shape, const Fan &f, const LineParams &base, int npaths, int sat,
                      bool ms, cudaStream_t st, Marker &mark, int even_only, uint8_t *disp, double Nout) {
     if (shape.sched == SGMGB_SCHED_LATENCY)
-        return run_planes(s, base, npaths, sat, ms, shape.wpb, st, mark, even_only, disp, Nout);
-    return run_final(s, base, npaths, sat, ms, shape.wpb, st, mark, even_only, disp, Nout);
+        return run_planes(f, base, npaths, sat, ms, shape.wpb, st, mark, even_only, disp, Nout);
+    return run_final(f, base, npaths, sat, ms, shape.wpb, st, mark, even_only, disp, Nout);
 }
 
 }  // namespace
@@ -383,37 +417,59 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
         p.C = s.C; p.sc = s.sc; p.S = s.S; p.disp = d_disp;
         p.W = fd.W; p.H = fd.H; p.D = fd.D; p.dpl = shape.dpl;
         p.p2 = 192; p.even_only = 0; p.p1 = 20;
-        if ((e = run_dirs(shape, s, p, fd.paths, 0, false, st, mark, 0, d_disp, N)) != cudaSuccess) return e;
+        if ((e = run_dirs(shape, main_fan(s, (size_t)ND), p, fd.paths, 0, false, st, mark, 0, d_disp, N)) !=
+            cudaSuccess)
+            return e;
     } else {
         const int W = fd.W, H = fd.H, hw = W / 2, hh = H / 2;
         const double Nh = (double)hw * hh, NhD = Nh * 64;
-        // stage 1: half scale (multiscale/sgm_ms_ref.c:168-181)
-        if ((e = launch_half2(d_left, d_right, s.halfL, s.halfR, W, H, st)) != cudaSuccess) return e;
+        // The half-scale stage (multiscale/sgm_ms_ref.c:168-181) runs on its own
+        // stream set beside the full-scale prefilters and stage: the full scale
+        // needs only its cost volume, in the cost merge; its map is defined work
+        // that nothing reads. With a probe attached everything runs on `st`, in
+        // the order below.
+        const bool serial = probe != nullptr;
+        cudaStream_t sm = serial ? st : s.ms;
+        if (!serial) {
+            if ((e = cudaEventRecord(s.fork_ms, st)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(sm, s.fork_ms, 0)) != cudaSuccess) return e;
+        }
+        if ((e = launch_half2(d_left, d_right, s.halfL, s.halfR, W, H, sm)) != cudaSuccess) return e;
         if ((e = mark("half", 2 * N + 2 * Nh)) != cudaSuccess) return e;
-        if ((e = launch_sobel2(s.halfL, s.halfR, s.hsobL, s.hsobR, hw, hh, st)) != cudaSuccess) return e;
+        if ((e = launch_sobel2(s.halfL, s.halfR, s.hsobL, s.hsobR, hw, hh, sm)) != cudaSuccess) return e;
         if ((e = mark("sobel_half", 4 * Nh)) != cudaSuccess) return e;
-        if ((e = launch_census2(s.hsobL, s.hsobR, s.cl1, s.cr1, hw, hh, st)) != cudaSuccess) return e;
+        if ((e = launch_census2(s.hsobL, s.hsobR, s.cl1, s.cr1, hw, hh, sm)) != cudaSuccess) return e;
         if ((e = mark("census_half", 18 * Nh)) != cudaSuccess) return e;
-        if ((e = launch_cost(s.cl1, s.cr1, s.C1, nullptr, hw, hh, 64, kInvalidMultiscale, st)) != cudaSuccess)
+        if ((e = launch_cost(s.cl1, s.cr1, s.C1, nullptr, hw, hh, 64, kInvalidMultiscale, sm)) != cudaSuccess)
             return e;
         if ((e = mark("cost_half", 16 * Nh + NhD)) != cudaSuccess) return e;
+        if (!serial && (e = cudaEventRecord(s.c1, sm)) != cudaSuccess) return e;
+        // the full-scale prefilters, beside the half-scale chain
         if ((e = launch_sobel2(d_left, d_right, s.sobL, s.sobR, W, H, st)) != cudaSuccess) return e;
         if ((e = mark("sobel", 4 * N)) != cudaSuccess) return e;
         if ((e = launch_census2(s.sobL, s.sobR, s.cl, s.cr, W, H, st)) != cudaSuccess) return e;
         if ((e = mark("census", 18 * N)) != cudaSuccess) return e;
+        if (!serial && (e = cudaStreamWaitEvent(st, s.c1, 0)) != cudaSuccess) return e;
         if ((e = launch_cost(s.cl, s.cr, s.C, s.C1, W, H, 64, kInvalidMultiscale, st)) != cudaSuccess)
             return e;
         if ((e = mark("cost_merge", 16 * N + NhD + ND)) != cudaSuccess) return e;
         if (ev_census && (e = cudaEventRecord(ev_census, st)) != cudaSuccess) return e;
+        // stage 1's path passes and map on the half-scale stream set, in its own planes
         LineParams p1{};
-        p1.C = s.C1; p1.sc = s.sc; p1.S = s.S; p1.disp = s.disp1;
+        p1.C = s.C1; p1.disp = s.disp1;
         p1.W = hw; p1.H = hh; p1.D = 64; p1.dpl = shape.dpl; p1.p2 = 200; p1.even_only = 0;
-        if ((e = run_dirs(shape, s, p1, 8, 1, true, st, mark, 0, s.disp1, Nh)) != cudaSuccess) return e;
+        if ((e = run_dirs(shape, half_fan(s, (size_t)NhD), p1, 8, 1, true, sm, mark, 0, s.disp1, Nh)) !=
+            cudaSuccess)
+            return e;
+        if (!serial && (e = cudaEventRecord(s.s1_done, sm)) != cudaSuccess) return e;
         // stage 2: full scale, cost averaged with the half-scale cost (:183-199)
         LineParams p2{};
         p2.C = s.C; p2.sc = s.sc; p2.S = s.S; p2.disp = d_disp;
         p2.W = W; p2.H = H; p2.D = 64; p2.dpl = shape.dpl; p2.p2 = 200; p2.even_only = 1;
-        if ((e = run_dirs(shape, s, p2, 8, 1, true, st, mark, 1, d_disp, Nh)) != cudaSuccess) return e;
+        if ((e = run_dirs(shape, main_fan(s, (size_t)ND), p2, 8, 1, true, st, mark, 1, d_disp, Nh)) !=
+            cudaSuccess)
+            return e;
+        if (!serial && (e = cudaStreamWaitEvent(st, s.s1_done, 0)) != cudaSuccess) return e;
     }
     if (ev_end && (e = cudaEventRecord(ev_end, st)) != cudaSuccess) return e;
     return cudaSuccess;
