@@ -158,6 +158,9 @@ __device__ __forceinline__ void item_path(const BPass &bp, uint8_t *disp, int wa
         case 4 * 8 + MODE_STORE:   path_pair<4, MODE_STORE, 0, false>(P, warp, ring); break;
         case 4 * 8 + MODE_ACCUM:   path_pair<4, MODE_ACCUM, 0, false>(P, warp, ring); break;
         case 4 * 8 + MODE_FINAL:   path_pair<4, MODE_FINAL, 0, false>(P, warp, ring); break;
+        case 1 * 8 + MODE_FINAL7:  path_pair<1, MODE_FINAL7, 0, false>(P, warp, ring); break;
+        case 2 * 8 + MODE_FINAL7:  path_pair<2, MODE_FINAL7, 0, false>(P, warp, ring); break;
+        case 4 * 8 + MODE_FINAL7:  path_pair<4, MODE_FINAL7, 0, false>(P, warp, ring); break;
         case 1 * 8 + MODE_FINAL3H: path_pair<1, MODE_FINAL3H, 0, true>(P, warp, ring); break;
         case 2 * 8 + MODE_FINAL3H: path_pair<2, MODE_FINAL3H, 0, true>(P, warp, ring); break;
         case 4 * 8 + MODE_FINAL3H: path_pair<4, MODE_FINAL3H, 0, false>(P, warp, ring); break;
@@ -268,6 +271,7 @@ int pair_ring_nr(int mode) {
     case MODE_STORE:   return PairSlot<NR, MODE_STORE>::RING;
     case MODE_ACCUM:   return PairSlot<NR, MODE_ACCUM>::RING;
     case MODE_FINAL:   return PairSlot<NR, MODE_FINAL>::RING;
+    case MODE_FINAL7:  return PairSlot<NR, MODE_FINAL7>::RING;
     default:           return PairSlot<NR, MODE_FINAL3>::RING;
     }
 }
@@ -452,7 +456,7 @@ int build_plan(sgmgb_batch *b) {
             bp.P.sc = sp.sc; bp.P.sc2 = sp.sc2; bp.P.sc3 = sp.sc3;
             for (int q = 0; q < 4; q++) bp.P.xpl[q] = xplanes[q];
             bp.P.nlines = lines_for(fd.W, fd.H, sp.dx, sp.dy);
-            const bool pair = fdpl == 0 && pair_ok(fd.D) && sp.mode != MODE_FINAL7;
+            const bool pair = fdpl == 0 && pair_ok(fd.D);
             bp.frame = f; bp.mode = sp.mode; bp.dpl = pair ? 0 : dpl;
             const int pi = (int)passes.size();
             passes.push_back(bp);

@@ -45,17 +45,18 @@ namespace {
 // 0.261). The other modes keep 512 bytes.
 template <int NR, int MODE> struct PairRing {
     static constexpr bool F3 = MODE == MODE_FINAL3 || MODE == MODE_FINAL3H;
+    static constexpr bool F7 = MODE == MODE_FINAL7;                // eight input streams: 512-byte chunks
     static constexpr int G = MODE == MODE_SCRATCH ? (NR == 4 ? 4 : 2) : (F3 ? 2 : 1);
     static constexpr int CB = 512 * G;                             // bytes of one stream per chunk
     static constexpr int K = 8 * G / NR;                           // steps per chunk
-    static constexpr int NCH = F3 ? 3 : (NR == 1 ? 4 : (NR == 2 ? 6 : 8));   // ring depth
+    static constexpr int NCH = (F3 || F7) ? 3 : (NR == 1 ? 4 : (NR == 2 ? 6 : 8));   // ring depth
     static constexpr int SB = 64 * NR;                             // bytes of one stream per step: [A | B]
 };
 // Streams of a chunk slot, in units of CB bytes: the cost bytes, the planes
-// the pass reads (one: sc; three for FINAL3), and the partial sum S (uint16,
-// two units) for ACCUM and FINAL.
+// the pass reads (one: sc; three for FINAL3; seven for FINAL7), and the
+// partial sum S (uint16, two units) for ACCUM and FINAL.
 template <int NR, int MODE> struct PairSlot {
-    static constexpr int NPL = MODE == MODE_SCRATCH ? 0 : (PairRing<NR, MODE>::F3 ? 3 : 1);
+    static constexpr int NPL = MODE == MODE_SCRATCH ? 0 : (PairRing<NR, MODE>::F3 ? 3 : (MODE == MODE_FINAL7 ? 7 : 1));
     static constexpr bool HAS_S = MODE == MODE_ACCUM || MODE == MODE_FINAL;
     static constexpr int U = 1 + NPL + (HAS_S ? 2 : 0);
     static constexpr int BYTES = PairRing<NR, MODE>::CB * U;
@@ -131,7 +132,8 @@ __device__ __forceinline__ void st_run(uint8_t *p, uint32_t v) {
 //   SCRATCH  L into the plane P.sc
 //   STORE    S = sc + L            ACCUM  S += sc + L
 //   FINAL    argmin(S + sc + L)    FINAL3 argmin(L + sc + sc2 + sc3) into P.disp
-// (the even-only map of the multi-scale variant in FINAL). SAT: clamp L to
+//   FINAL7   argmin(L + sc + sc2 + sc3 + xpl[0..3]) (8 paths)
+// (the even-only map of the multi-scale variant in FINAL and FINAL7). SAT: clamp L to
 // 255 (multiscale/sgm_ms_ref.c:82). `ring`: this warp's PairSlot<NR, MODE>::RING
 // bytes of shared memory (16-byte aligned). All 32 lanes must call it.
 template <int NR, int MODE, int SAT, bool KEY16>
@@ -142,7 +144,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     constexpr bool HAS_S = PairSlot<NR, MODE>::HAS_S;
     constexpr int SLOT = PairSlot<NR, MODE>::BYTES;
     constexpr int D = 32 * NR;
-    constexpr bool FIN = MODE == MODE_FINAL || MODE == MODE_FINAL3 || MODE == MODE_FINAL3H;
+    constexpr bool FIN = MODE == MODE_FINAL || MODE == MODE_FINAL3 || MODE == MODE_FINAL3H || MODE == MODE_FINAL7;
     constexpr int KW = (K + 3) / 4;                   // FINAL3H: words of one row's disparities per chunk
     const int lane = threadIdx.x & 31;
     const int la = 2 * warp;
@@ -191,7 +193,8 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     const uint8_t *src[1 + NPL];
     src[0] = P.C;
     if (NPL >= 1) src[1] = P.sc;
-    if (NPL == 3) { src[2] = P.sc2; src[3] = P.sc3; }
+    if (NPL >= 3) { src[2] = P.sc2; src[3] = P.sc3; }
+    if (NPL == 7) { src[4] = P.xpl[0]; src[5] = P.xpl[1]; src[6] = P.xpl[2]; src[7] = P.xpl[3]; }
     auto issue = [&](int c) {
         const uint32_t dst = ring_s + (uint32_t)((c % NCH) * SLOT);
 #pragma unroll
@@ -337,7 +340,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             return;
         }
         if (lane == 0) {
-            if (MODE == MODE_FINAL && P.even_only) {  // multi-scale: the map at (2x, 2y) only
+            if ((MODE == MODE_FINAL || MODE == MODE_FINAL7) && P.even_only) {   // multi-scale: the map at (2x, 2y) only
                 if (live_a && !((xa | ya) & 1)) P.disp[(long long)(ya >> 1) * hw + (xa >> 1)] = (uint8_t)da;
                 if (live_b && !((xb | yb) & 1)) P.disp[(long long)(yb >> 1) * hw + (xb >> 1)] = (uint8_t)db;
             } else if (pair_store) {
