@@ -165,6 +165,20 @@ __device__ __forceinline__ uint64_t ld_desc(const uint64_t *p) {
     return LD_CG ? __ldcg(p) : __ldg(p);
 }
 
+// Bytewise (a + b + 1) >> 1 of four packed bytes: a + b = 2(a | b) - (a ^ b),
+// so the rounded-up half is (a | b) - ((a ^ b) >> 1), with the shift kept
+// inside each byte; no byte borrows, since (a ^ b) >> 1 <= a | b.
+__device__ __forceinline__ uint32_t avg_up_u8x4(uint32_t a, uint32_t b) {
+    return (a | b) - (((a ^ b) >> 1) & 0x7F7F7F7Fu);
+}
+
+// The multi-scale merge of 8 packed costs d0..d0+7 of a full-scale pixel
+// with the half-scale costs at d/2: h holds c1[d0/2 .. d0/2 + 3], and cost
+// d0 + k averages with byte k >> 1 (multiscale/sgm_ms_ref.c:184-188).
+__device__ __forceinline__ uint2 merge_half(uint32_t lo, uint32_t hi, uint32_t h) {
+    return make_uint2(avg_up_u8x4(lo, __byte_perm(h, 0, 0x1100)), avg_up_u8x4(hi, __byte_perm(h, 0, 0x3322)));
+}
+
 // One pixel's 8 costs d0..d0+7 from staged descriptors; r[-k] = cr[x - d0 - k].
 // EDGE: some x - d0 - k may be negative (the first D columns of a row).
 template <bool EDGE>
@@ -196,14 +210,13 @@ __device__ __forceinline__ void cost_tasks(const uint64_t *sl, const uint64_t *s
         if (TAIL && x >= W) continue;
         uint32_t v[8];
         cost8<EDGE>(sl[px], sr + px + (D - 1) - d0, x, d0, invalid, v);
-        if (MS) {   // full scale of the multi-scale variant
-            const uint32_t h = *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + (x >> 1)) * D + (d0 >> 1));
-#pragma unroll
-            for (int k = 0; k < 8; k++) v[k] = (v[k] + ((h >> (8 * (k >> 1))) & 0xFFu) + 1) >> 1;
-        }
         const uint32_t lo = v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24);
         const uint32_t hi = v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24);
-        *(uint2 *)(row + (size_t)x * D + d0) = make_uint2(lo, hi);
+        if (MS)     // full scale of the multi-scale variant
+            *(uint2 *)(row + (size_t)x * D + d0) =
+                merge_half(lo, hi, *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + (x >> 1)) * D + (d0 >> 1)));
+        else
+            *(uint2 *)(row + (size_t)x * D + d0) = make_uint2(lo, hi);
     }
 }
 
@@ -239,14 +252,13 @@ __device__ __forceinline__ void cost_pairs(const uint64_t *sl, const uint64_t *s
             uint32_t v[8];
 #pragma unroll
             for (int k = 0; k < 8; k++) v[k] = (uint32_t)__popcll(a[i] ^ r[7 + i - k]);
-            if (MS) {   // full scale of the multi-scale variant: x is even, pixel pairs share (x/2, y/2)
-                const uint32_t h =
-                    *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + ((x + i) >> 1)) * D + (d0 >> 1));
-#pragma unroll
-                for (int k = 0; k < 8; k++) v[k] = (v[k] + ((h >> (8 * (k >> 1))) & 0xFFu) + 1) >> 1;
-            }
-            *(uint2 *)(row + (size_t)(x + i) * D + d0) = make_uint2(v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24),
-                                                                    v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24));
+            const uint32_t lo = v[0] | (v[1] << 8) | (v[2] << 16) | (v[3] << 24);
+            const uint32_t hi = v[4] | (v[5] << 8) | (v[6] << 16) | (v[7] << 24);
+            if (MS)     // full scale of the multi-scale variant: x is even, pixel pairs share (x/2, y/2)
+                *(uint2 *)(row + (size_t)(x + i) * D + d0) = merge_half(
+                    lo, hi, *(const uint32_t *)(C1 + ((size_t)(y >> 1) * hw + ((x + i) >> 1)) * D + (d0 >> 1)));
+            else
+                *(uint2 *)(row + (size_t)(x + i) * D + d0) = make_uint2(lo, hi);
         }
     }
 }
