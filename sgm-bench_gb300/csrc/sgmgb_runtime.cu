@@ -142,12 +142,6 @@ const char *pass_name(int dx, int dy) {
     return dy > 0 ? "path_diag_tr_bl" : "path_diag_br_tl";
 }
 
-// The THROUGHPUT schedule: every direction but T->B parks its L in its own
-// plane (the same planes as run_planes, one fewer), side by side on forked
-// streams; then T->B adds them to its own L and takes the argmin
-// (MODE_FINAL3 for 4 paths, MODE_FINAL7 for 8). One plane less is written
-// and read than with run_planes, at the price of a long pass on the frame's
-// critical path.
 // The forked streams, events and direction planes of one group of path
 // passes: the frame's own (main_fan), or, for the half-scale stage of a
 // multi-scale frame, which runs beside the full-scale stage, a set of its own
@@ -170,6 +164,12 @@ Fan half_fan(const FrameSlot &s, size_t plane) {
     return f;
 }
 
+// The THROUGHPUT schedule: every direction but T->B parks its L in its own
+// plane (the same planes as run_planes, one fewer), side by side on forked
+// streams; then T->B adds them to its own L and takes the argmin
+// (MODE_FINAL3 for 4 paths, MODE_FINAL7 for 8). One plane less is written
+// and read than with run_planes, at the price of a long pass on the frame's
+// critical path.
 cudaError_t run_final(const Fan &f, const LineParams &base, int npaths, int sat, bool ms, int wpb,
                       cudaStream_t st, Marker &mark, int even_only, uint8_t *disp, double Nout) {
     const bool serial = mark.pr != nullptr;

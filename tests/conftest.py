@@ -40,6 +40,17 @@ def reference_plain(left, right, D, paths):
     return oracle.plain(left, right, D, paths)
 
 
+def reference_multiscale_hash(left, right):
+    """The checker's FNV-1a-64 of a multi-scale frame's map: the reference's own
+    multiscale/sgm_ms_ref.c (built into oracle/_ref, on all host threads) where
+    it is built, else the oracle restating it."""
+    import oracle
+    try:
+        return oracle.reference_multiscale(left, right, reps=1)[1]
+    except FileNotFoundError:
+        return oracle.fnv1a64(oracle.multiscale(left, right))
+
+
 # Frames at the sizes of the batched and served configurations: 1920x1080 D=128
 # 8-path, 1920x800 D=64 8-path and 1280x720 D=128 4-path.
 BASELINE_FRAMES = [(1920, 1080, 128, 8), (1920, 800, 64, 8), (1280, 720, 128, 4)]

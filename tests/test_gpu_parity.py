@@ -106,6 +106,33 @@ def test_multiscale_synthetic(engine):
     assert np.array_equal(got, oracle.multiscale(left, right))
 
 
+@pytest.mark.parametrize("sched", ["latency", "throughput"])
+def test_multiscale_async_graph(engine, sched):
+    """The device-buffer call captures the frame into a CUDA graph, the
+    half-scale stage on its own streams beside the full-scale one: the
+    captured frame, replayed on two buffer sets, gives the oracle's maps."""
+    import torch
+    from conftest import reference_multiscale_hash
+    engine.set_schedule(SCHEDS[sched])
+    try:
+        for W, H in ((320, 200), (1920, 800)):
+            engine.plan(W, H, 64, 8, sgmgb.MULTISCALE)
+            pairs = [sgmgb.synth_pair(W, H, 64, seed=W + k)[:2] for k in range(2)]
+            wants = [reference_multiscale_hash(l, r) for l, r in pairs]
+            dl = [torch.from_numpy(l).cuda() for l, r in pairs]
+            dr = [torch.from_numpy(r).cuda() for l, r in pairs]
+            dd = [torch.zeros((H // 2, W // 2), dtype=torch.uint8, device="cuda") for _ in pairs]
+            for rep in range(3):                             # capture, then replays
+                for k in range(2):
+                    engine.run_frame_async(dl[k], dr[k], dd[k])
+                engine.sync()
+                for k in range(2):
+                    assert oracle.fnv1a64(dd[k].cpu().numpy()) == wants[k], (W, H, sched, rep, k)
+                    dd[k].zero_()
+    finally:
+        engine.set_schedule(sgmgb.SCHED_AUTO)
+
+
 # ---- path-kernel shapes: only speed may depend on them ----
 @pytest.mark.parametrize("wpb,dpl", [(1, 2), (2, 4), (3, 8), (4, 4), (4, 8)])
 def test_path_shapes(engine, wpb, dpl):
