@@ -39,6 +39,8 @@ struct LineParams {
     int nlines;                  // independent lines for this direction
     int even_only;               // multi-scale full scale: only lines through even (x, y) (nlines from
                                  // lines_for_even), SCRATCH stores and final argmins only at even (x, y),
+                                 // the planes compact (pixel (x, y) at (y/2)(W/2) + x/2; SCRATCH and
+                                 // FINAL7 only),
                                  // the map (W/2)x(H/2)
     int key16;                   // final: S*64 + d fits 16 bits (4 paths, D <= 64)
     int dpl;                     // disparities per lane: 2, 4 or 8; 0 picks the smallest valid
@@ -123,7 +125,7 @@ cudaError_t prepare_fused_kernels();
 // layout (16-byte aligned).
 struct SumPlanes { const uint8_t *p[8]; };
 // disp = argmin_d of the sum of the np (4 or 8) planes, lowest d on ties;
-// even_only: at even (x, y) only, into a (W/2)x(H/2) map (sgmgb_sum.cu).
+// even_only: at even (x, y) only, from compact planes, into a (W/2)x(H/2) map (sgmgb_sum.cu).
 cudaError_t launch_sum(const SumPlanes &pl, int np, uint8_t *disp, int W, int H, int D, int even_only,
                        cudaStream_t s);
 

@@ -169,6 +169,9 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     // b / (2 SB), line b % (2 SB) / (2D), byte b % (2D).
     const uint32_t ring_s = (uint32_t)__cvta_generic_to_shared(ring);
     const long long adv = (long long)K * step * D;
+    // even_only planes are compact: the pixel (x, y), x and y even, at
+    // (y/2)(W/2) + x/2; two steps along any direction move (dy W/2 + dx) there
+    const long long oadv = P.even_only ? (long long)(K / 2) * (dy * (P.W >> 1) + dx) * D : adv;
     long long goff[G], ooff[G];
     int glim[G];
     bool ost[G];
@@ -177,10 +180,12 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         const int gb = (lane + 32 * h) * 16, gk = gb / SB, gr = gb % SB, gl = gr / D, go = gr - gl * D;
         goff[h] = ((long long)(gl ? pb : pa) + (long long)gk * step) * D + go;
         glim[h] = (gl ? lenb : lena) - gk;
-        ooff[h] = goff[h];                            // scratch output: same granules, plane P.sc
-        // even_only: only pixels with x and y both even are stored (a chunk is
-        // an even number of steps: a granule's parity is the same in every chunk)
-        ost[h] = !P.even_only || ((((gl ? xb : xa) + gk * dx) | ((gl ? yb : ya) + gk * dy)) & 1) == 0;
+        // scratch output: the same granules, into plane P.sc. even_only: only
+        // pixels with x and y both even are stored (a chunk is an even number of
+        // steps: a granule's parity is the same in every chunk), compact
+        const int gx = (gl ? xb : xa) + gk * dx, gy = (gl ? yb : ya) + gk * dy;
+        ost[h] = !P.even_only || ((gx | gy) & 1) == 0;
+        ooff[h] = P.even_only ? ((long long)(gy >> 1) * (P.W >> 1) + (gx >> 1)) * D + go : goff[h];
     }
     long long soff[2 * G];
     int slim[2 * G];
@@ -424,7 +429,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
             for (int h = 0; h < G; h++) {
                 if (ost[h] && ch * K < glim[h])
                     *(uint4 *)(P.sc + ooff[h]) = *(const uint4 *)(chunk + (lane + 32 * h) * 16);
-                ooff[h] += adv;
+                ooff[h] += oadv;
             }
         }
     }

@@ -5,12 +5,13 @@
 
 namespace sgmgb {
 
-template <int DPL, int MODE, int SAT, bool KEY16>
+template <int DPL, int MODE, int SAT, bool KEY16, bool EO = false>
 __global__ void __launch_bounds__(128)
 k_path(const LineParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     const int wib = threadIdx.x >> 5;
-    path_warp<DPL, MODE, SAT, KEY16>(P, blockIdx.x * (blockDim.x >> 5) + wib, smem + wib * Slot<DPL, MODE>::RING);
+    path_warp<DPL, MODE, SAT, KEY16, EO>(P, blockIdx.x * (blockDim.x >> 5) + wib,
+                                         smem + wib * Slot<DPL, MODE>::RING);
 }
 
 template <int NR, int MODE, int SAT, bool KEY16>
@@ -63,6 +64,7 @@ static cudaError_t launch_pair_one(const LineParams &p, int wpb, cudaStream_t s)
 // any mode.
 static bool pair_applies(const LineParams &p, int mode, int saturate) {
     if (p.dpl != 0 || (p.D != 32 && p.D != 64 && p.D != 128)) return false;
+    if (p.even_only && mode != MODE_SCRATCH) return false;   // its finals read the planes in the full layout
     if (mode == MODE_SCRATCH) return !saturate || p.D == 64;   // the multi-scale passes (saturating, D = 64)
     return (mode == MODE_FINAL3 || mode == MODE_FINAL3H || mode == MODE_FINAL7) && !saturate;
 }
@@ -106,11 +108,11 @@ static cudaError_t launch_pair(const LineParams &p, int mode, int saturate, int 
     }
 }
 
-template <int DPL, int MODE, int SAT, bool KEY16>
+template <int DPL, int MODE, int SAT, bool KEY16, bool EO = false>
 static cudaError_t prep_one() {
-    cudaError_t e = cudaFuncSetAttribute(k_path<DPL, MODE, SAT, KEY16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         4 * Slot<DPL, MODE>::RING);
-    if (e == cudaSuccess) e = set_carveout(k_path<DPL, MODE, SAT, KEY16>);
+    cudaError_t e = cudaFuncSetAttribute(k_path<DPL, MODE, SAT, KEY16, EO>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * Slot<DPL, MODE>::RING);
+    if (e == cudaSuccess) e = set_carveout(k_path<DPL, MODE, SAT, KEY16, EO>);
     return e;
 }
 
@@ -147,6 +149,7 @@ cudaError_t prepare_path_kernels() {
     if ((e = prep_dpl<4, 0, true>()) != cudaSuccess) return e;
     if ((e = prep_dpl<8, 0, false>()) != cudaSuccess) return e;
     if ((e = prep_dpl<2, 1, false>()) != cudaSuccess) return e;
+    if ((e = prep_one<2, MODE_FINAL7, 1, false, true>()) != cudaSuccess) return e;   // the multi-scale T->B final
     if ((e = prep_dpl<4, 1, false>()) != cudaSuccess) return e;
     return prep_dpl<8, 1, false>();
 }
@@ -166,7 +169,12 @@ static cudaError_t launch_path_mode(const LineParams &p, int mode, dim3 g, dim3 
     case MODE_FINAL3:
         k_path<DPL, MODE_FINAL3, SAT, KEY16><<<g, b, w * Slot<DPL, MODE_FINAL3>::RING, s>>>(p); break;
     case MODE_FINAL7:
-        k_path<DPL, MODE_FINAL7, SAT, false><<<g, b, w * Slot<DPL, MODE_FINAL7>::RING, s>>>(p); break;
+        // the multi-scale full scale's T->B final: even columns from row 0, one line per warp
+        if (SAT && DPL == 2 && p.even_only && p.gpw == 1 && p.dx == 0 && p.dy == 1)
+            k_path<2, MODE_FINAL7, 1, false, true><<<g, b, w * Slot<2, MODE_FINAL7>::RING, s>>>(p);
+        else
+            k_path<DPL, MODE_FINAL7, SAT, false><<<g, b, w * Slot<DPL, MODE_FINAL7>::RING, s>>>(p);
+        break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

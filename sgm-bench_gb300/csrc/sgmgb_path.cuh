@@ -301,7 +301,11 @@ __device__ __forceinline__ void emit(const LineParams &P, void *out, int p, int 
 // (P.dx, P.dy), with P.nl/P.lpl/P.gpw set for DPL. `ring` is this warp's
 // Slot<DPL, MODE>::RING bytes of shared memory (16-byte aligned). All 32 lanes
 // of the warp must call it.
-template <int DPL, int MODE, int SAT, bool KEY16>
+// EO (FINAL7 only): the even-only final down the even columns from row 0 (the
+// multi-scale full scale's T->B final, one line per warp): its odd rows'
+// argmins are not kept, so those steps run the recurrence alone (the
+// launcher picks EO only for such a pass).
+template <int DPL, int MODE, int SAT, bool KEY16, bool EO = false>
 __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t *ring) {
     constexpr int NR = DPL / 2;
     constexpr int K = Ring<DPL, MODE>::K, SBM = Ring<DPL, MODE>::SBM, NGB = Ring<DPL, MODE>::NGB,
@@ -356,15 +360,21 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
     // SCRATCH: the plane has the cost volume's layout, so the chunk's L bytes,
     // staged where its cost bytes were, go out by the same 16-byte granules.
     // even_only: only the granules of pixels with x and y even (a chunk is an
-    // even number of steps, so a granule's parity is the same in every chunk).
-    long long ooff[NGB];
+    // even number of steps, so a granule's parity is the same in every chunk),
+    // into a compact plane: pixel (x, y) at (y/2)(W/2) + x/2, where two steps
+    // along any direction move (dy W/2 + dx). The even-only final reads its
+    // planes there (poff).
+    const long long oadv = P.even_only ? (long long)(K / 2) * (dy * (P.W >> 1) + dx) * P.D : adv;
+    long long ooff[NGB], poff[NGB];
     bool ost[NGB];
 #pragma unroll
     for (int j = 0; j < NGB; j++) {
-        ooff[j] = goff[j];
-        const int b = (lane + 32 * j) * 16, k = b / SBM, gg = min((b % SBM) / P.D, 31);
-        const int xg = __shfl_sync(kFull, x, (gg * LPL) & 31), yg = __shfl_sync(kFull, y, (gg * LPL) & 31);
-        ost[j] = !P.even_only || (((xg + k * dx) | (yg + k * dy)) & 1) == 0;
+        const int b = (lane + 32 * j) * 16, k = b / SBM, gg = min((b % SBM) / P.D, 31), o = b % SBM - gg * P.D;
+        const int xg = __shfl_sync(kFull, x, (gg * LPL) & 31) + k * dx;
+        const int yg = __shfl_sync(kFull, y, (gg * LPL) & 31) + k * dy;
+        ost[j] = !P.even_only || ((xg | yg) & 1) == 0;
+        ooff[j] = P.even_only ? ((long long)(yg >> 1) * (P.W >> 1) + (xg >> 1)) * P.D + o : goff[j];
+        poff[j] = ooff[j];
     }
     long long soff[HAS_S ? 2 * NGB : 1];
     int slim[HAS_S ? 2 * NGB : 1];
@@ -397,10 +407,11 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
                 // those pixels' argmins are kept, so the other granules' planes are not read
                 if (ost[j]) {
 #pragma unroll
-                    for (int q = 0; q < NPL; q++) cp_async16(db + (uint32_t)((1 + q) * K * SBM), pl[q] + goff[j]);
+                    for (int q = 0; q < NPL; q++) cp_async16(db + (uint32_t)((1 + q) * K * SBM), pl[q] + poff[j]);
                 }
             }
             goff[j] += adv;
+            poff[j] += oadv;
         }
         if (HAS_S) {
 #pragma unroll
@@ -453,9 +464,10 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
     // One recurrence step on the next pixel of the line; FULL: every line of
     // the warp has this pixel (no per-step length test); ONE: the warp holds
     // one line (a plain full-warp reduction).
-    auto step_once = [&](const In &s, int i, uint8_t *stage, auto full_t, auto one_t) {
+    auto step_once = [&](const In &s, int i, uint8_t *stage, auto full_t, auto one_t, auto emit_t) {
         constexpr bool FULL = decltype(full_t)::value;
         constexpr bool ONE = decltype(one_t)::value;
+        constexpr bool EMIT = decltype(emit_t)::value;   // false: the recurrence only (no output at this pixel)
         x += dx; y += dy; p += step;
         if (MODE == MODE_STORE || MODE == MODE_ACCUM) out += out_step;
         const bool live = MODE == MODE_SCRATCH ? has_d : (FULL ? active : i < len);
@@ -498,9 +510,15 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
             tm = vmin2(tm, v);
         }
         mn = ONE ? __reduce_min_sync(kFull, fold2(tm)) : group_min(fold2(tm), G, g, gmask);
-        emit<DPL, MODE, KEY16, ONE>(P, MODE == MODE_SCRATCH ? (void *)stage : (void *)out, p, x, y, d0, lead, g,
-                                    gmask, live, L, s);
+        if (EMIT)
+            emit<DPL, MODE, KEY16, ONE>(P, MODE == MODE_SCRATCH ? (void *)stage : (void *)out, p, x, y, d0, lead,
+                                        g, gmask, live, L, s);
     };
+
+    // EO: the line starts at an even row of an even column and a chunk is an
+    // even number of steps, so a chunk's odd steps are the odd rows, whose
+    // argmins are not kept; they run the recurrence on the cost alone, without
+    // the planes, the sum or the argmin
 
     // the chunk loop, instantiated for one line per warp and for several
     auto run = [&](auto one_t) {
@@ -510,21 +528,21 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
             issue(ch + NCH - 1);
             uint8_t *chunk = ring + (ch % NCH) * SLOT;
             if (MODE == MODE_FINAL7) {  // eight input streams: read each step's inputs when it runs
-                if ((ch + 1) * K <= minlen) {
+                auto steps = [&](auto full_t) {
 #pragma unroll
                     for (int k = 0; k < K; k++) {
                         In s1;
-                        ring_read<DPL, MODE>(chunk, lane, k, s1);
-                        step_once(s1, ch * K + k, chunk + k * SBM + lane * DPL, std::true_type{}, one_t);
+                        if (EO && (k & 1)) {
+                            load_bytes<DPL>(chunk + k * SBM + lane * DPL, s1.cw);
+                            step_once(s1, ch * K + k, chunk + k * SBM + lane * DPL, full_t, one_t, std::false_type{});
+                        } else {
+                            ring_read<DPL, MODE>(chunk, lane, k, s1);
+                            step_once(s1, ch * K + k, chunk + k * SBM + lane * DPL, full_t, one_t, std::true_type{});
+                        }
                     }
-                } else {
-#pragma unroll
-                    for (int k = 0; k < K; k++) {
-                        In s1;
-                        ring_read<DPL, MODE>(chunk, lane, k, s1);
-                        step_once(s1, ch * K + k, chunk + k * SBM + lane * DPL, std::false_type{}, one_t);
-                    }
-                }
+                };
+                if ((ch + 1) * K <= minlen) steps(std::true_type{});
+                else steps(std::false_type{});
                 continue;
             }
             In s[K];                    // the chunk's inputs, read before its steps run
@@ -533,11 +551,13 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
             if ((ch + 1) * K <= minlen) {
 #pragma unroll
                 for (int k = 0; k < K; k++)
-                    step_once(s[k], ch * K + k, chunk + k * SBM + lane * DPL, std::true_type{}, one_t);
+                    step_once(s[k], ch * K + k, chunk + k * SBM + lane * DPL, std::true_type{}, one_t,
+                              std::true_type{});
             } else {
 #pragma unroll
                 for (int k = 0; k < K; k++)
-                    step_once(s[k], ch * K + k, chunk + k * SBM + lane * DPL, std::false_type{}, one_t);
+                    step_once(s[k], ch * K + k, chunk + k * SBM + lane * DPL, std::false_type{}, one_t,
+                              std::true_type{});
             }
             if (MODE == MODE_SCRATCH) {
                 __syncwarp();           // every lane's L bytes of the chunk are staged
@@ -545,7 +565,7 @@ __device__ __forceinline__ void path_warp(const LineParams &P, int warp, uint8_t
                 for (int j = 0; j < NGB; j++) {
                     if (ost[j] && ch * K < glim[j])
                         *(uint4 *)(P.sc + ooff[j]) = *(const uint4 *)(chunk + (lane + 32 * j) * 16);
-                    ooff[j] += adv;
+                    ooff[j] += oadv;
                 }
             }
         }

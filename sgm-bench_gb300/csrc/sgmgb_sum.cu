@@ -29,7 +29,8 @@ __device__ __forceinline__ uint32_t vminu2(uint32_t a, uint32_t b) {
     return r;
 }
 
-// EVEN: only pixels (2ox, 2oy), output (W/2)x(H/2). Grid: (ceil(ow / npb), oh).
+// EVEN: only pixels (2ox, 2oy), output (W/2)x(H/2), from compact planes (the
+// even-only passes store pixel (2ox, 2oy) at oy*(W/2) + ox). Grid: (ceil(ow / npb), oh).
 // lt: log2(D/16) when SHFL (D/16 divides 32); npb: pixels per block.
 template <int NP, bool KEY16, bool SHFL, bool EVEN>
 __global__ void __launch_bounds__(256) k_sum(SumPlanes pl, uint8_t *__restrict__ disp, int W, int D, int tpp,
@@ -43,7 +44,7 @@ __global__ void __launch_bounds__(256) k_sum(SumPlanes pl, uint8_t *__restrict__
     const bool live = lp < npb && ox < ow;
     uint32_t key = 0xFFFFFFFFu;
     if (live) {
-        const size_t p = EVEN ? (size_t)(2 * oy) * W + 2 * ox : (size_t)oy * W + ox;
+        const size_t p = (size_t)oy * ow + ox;   // EVEN: the planes are compact, pixel (2ox, 2oy) at oy*ow + ox
         const size_t off = p * D + 16 * g;
         uint4 v[NP];
 #pragma unroll
