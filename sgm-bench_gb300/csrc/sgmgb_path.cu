@@ -37,9 +37,7 @@ static cudaError_t prep_pair_modes() {
     if ((e = prep_pair<NR, MODE_SCRATCH, SAT, false>()) != cudaSuccess) return e;
     if ((e = prep_pair<NR, MODE_STORE, SAT, false>()) != cudaSuccess) return e;
     if ((e = prep_pair<NR, MODE_ACCUM, SAT, false>()) != cudaSuccess) return e;
-    if constexpr (!SAT) {
-        if ((e = prep_pair<NR, MODE_FINAL7, 0, false>()) != cudaSuccess) return e;
-    }
+    if ((e = prep_pair<NR, MODE_FINAL7, SAT, false>()) != cudaSuccess) return e;
     return prep_pair<NR, MODE_FINAL, SAT, false>();
 }
 
@@ -52,21 +50,22 @@ static cudaError_t launch_pair_one(const LineParams &p, int wpb, cudaStream_t s)
 }
 
 // The pair layout (two lines per warp in register halves, sgmgb_pair.cuh)
-// serves the scratch passes at D = 32, 64 and 128 (the multi-scale ones,
-// saturating, at D = 64) and the plain finals of three and seven planes,
-// unless a disparities-per-lane shape was asked for. Alone, a pair pass is
-// slower (half the warps: multi-scale full-scale R->L 57 -> 70 us); side by
-// side with the other directions its halved instruction count wins
+// serves the scratch passes and the eight-plane final at D = 32, 64 and 128
+// (the multi-scale ones, saturating, at D = 64) and the plain three-plane
+// finals, unless a disparities-per-lane shape was asked for. Alone, a pair
+// pass is slower (half the warps: multi-scale full-scale R->L 57 -> 70 us);
+// side by side with the other directions its halved instruction count wins
 // (configuration C with 4 frames in flight 0.578 -> 0.535 ms). The
-// multi-scale final keeps one line per warp: its even columns give a pair
-// final only 480 warps at 1080p (226 against 147 us alone, and 0.494 against
-// 0.485 ms per frame with four in flight). The batch kernel may choose it for
-// any mode.
+// multi-scale full scale's final keeps one line per warp: its even columns
+// give a pair final only 480 warps at 1080p (226 against 147 us alone, and
+// 0.494 against 0.485 ms per frame with four in flight), and it skips its odd
+// rows' argmins (k_path's EO variant). The batch kernel may choose it for any
+// mode.
 static bool pair_applies(const LineParams &p, int mode, int saturate) {
     if (p.dpl != 0 || (p.D != 32 && p.D != 64 && p.D != 128)) return false;
     if (p.even_only && mode != MODE_SCRATCH) return false;   // its finals read the planes in the full layout
-    if (mode == MODE_SCRATCH) return !saturate || p.D == 64;   // the multi-scale passes (saturating, D = 64)
-    return (mode == MODE_FINAL3 || mode == MODE_FINAL3H || mode == MODE_FINAL7) && !saturate;
+    if (mode == MODE_SCRATCH || mode == MODE_FINAL7) return !saturate || p.D == 64;   // saturating: D = 64
+    return (mode == MODE_FINAL3 || mode == MODE_FINAL3H) && !saturate;
 }
 
 template <int NR, int SAT>
@@ -76,7 +75,7 @@ static cudaError_t launch_pair_nr(const LineParams &p, int mode, int wpb, cudaSt
     case MODE_STORE:   return launch_pair_one<NR, MODE_STORE, SAT, false>(p, wpb, s);
     case MODE_ACCUM:   return launch_pair_one<NR, MODE_ACCUM, SAT, false>(p, wpb, s);
     case MODE_FINAL:   return launch_pair_one<NR, MODE_FINAL, SAT, false>(p, wpb, s);
-    case MODE_FINAL7:  return SAT ? cudaErrorInvalidValue : launch_pair_one<NR, MODE_FINAL7, 0, false>(p, wpb, s);
+    case MODE_FINAL7:  return launch_pair_one<NR, MODE_FINAL7, SAT, false>(p, wpb, s);
     default:           return cudaErrorInvalidValue;
     }
 }
