@@ -56,12 +56,7 @@ METRIC = "MDE/s (W*H*D per second), 1080p D=64 4-path, bit-exact"
 UNIT = "MDE/s"
 B_ALG = 2 * W * H * D + 3 * W * H          # modelled minimal bytes per frame
 KERNELS_PER_FRAME = 2 + PATHS               # census + cost volume + one pass per direction
-
-
-def alone_sched(sgmgb):
-    """The schedule SGMGB_SCHED_AUTO gives a frame of this workload that has
-    the GPU to itself (the synchronous call): SPLIT from 2 Mpixel at D >= 64."""
-    return sgmgb.SCHED_SPLIT if W * H >= 2000000 and D >= 64 and PATHS == 4 else sgmgb.SCHED_LATENCY
+SCHED_NAMES = {1: "latency", 2: "throughput", 3: "fused", 4: "split"}
 
 
 def peaks():
@@ -641,9 +636,10 @@ def run_gb300(args):
             engines[i % nf].run_frame_async(dl[i % R], dr[i % R], dd[i % R], stream=streams[i % nf])
 
     # one frame at a time (a single context and stream), for the frame latency,
-    # with the schedule the synchronous call takes under AUTO for a frame alone
-    # of this size (SPLIT: at least 2 Mpixel at D >= 64)
-    eng.set_schedule(alone_sched(sgmgb))
+    # with the schedule the synchronous call takes under AUTO (the fastest for a
+    # frame alone, timed at the first call)
+    alone = eng.alone_schedule()
+    eng.set_schedule(alone)
     run_frames(3, 1)
     torch.cuda.synchronize(dev)
     e0s, e1s = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -685,7 +681,8 @@ def run_gb300(args):
     value = replica_value(ws, args.steps, ms / 1e3)
 
     # end to end through the host-buffer call: pinned inputs in, the map out
-    # into a pinned buffer, every step (the kernels move both across C2C)
+    # into a pinned buffer, every step (copied by the copy engines around the
+    # frame's CUDA graph)
     hl = [torch.from_numpy(p[0]).pin_memory().numpy() for p in pairs]
     hr = [torch.from_numpy(p[1]).pin_memory().numpy() for p in pairs]
     ho = [torch.empty((H, W), dtype=torch.uint8).pin_memory().numpy() for _ in range(2)]
@@ -730,7 +727,7 @@ def run_gb300(args):
     # stream: the fused schedule (`value`) and the one of a frame alone (`e2e`)
     eng.set_schedule(sgmgb.SCHED_FUSED)
     kstats = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
-    eng.set_schedule(alone_sched(sgmgb))
+    eng.set_schedule(alone)
     kstats_lat = eng.profile_frame(dl[0], dr[0], dd[0], reps=20)
     eng.set_schedule(sgmgb.SCHED_AUTO)
 
@@ -764,9 +761,10 @@ def run_gb300(args):
                 "fps": ws * e2e_steps / e2e_s, "p50_ms": statistics.median(lat) * 1e3,
                 "p99_ms": sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
                 "stage_ms": {k: round(v, 4) for k, v in st.items() if k.endswith("_ms")},
-                "schedule": "split (auto for one 1920x1080 D=64 frame at a time)",
-                "transfers": "pinned host buffers: the census kernel reads both images across NVLink-C2C inside "
-                             "the call; the map comes back with one copy",
+                "schedule": SCHED_NAMES.get(alone, "?") + " (auto: fastest for a frame alone, timed at the "
+                            "first call)",
+                "transfers": "pinned host buffers: both images copied in and the map copied back by the copy "
+                             "engines, the frame between them one CUDA graph, inside the call",
                 "same_map_as_device_path": e2e_exact,
                 "pageable": {"value": replica_value(ws, e2e_steps, pg_s), "unit": UNIT,
                              "fps": ws * e2e_steps / pg_s, "p50_ms": statistics.median(lat_pg) * 1e3,

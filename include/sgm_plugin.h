@@ -22,9 +22,9 @@ extern "C" {
 
 /* Same fields, order and types as common/sgm.h:9-25. */
 typedef struct {
-    double census_ms;     /* census and the cost volume */
-    double cost_ms;       /* -1: timed with the census (census_ms covers both) */
-    double aggregate_ms;
+    double census_ms;     /* -1: the census runs inside the frame's one graph (aggregate_ms) */
+    double cost_ms;       /* -1: likewise */
+    double aggregate_ms;  /* the whole frame on the device: census, cost, paths, argmin */
     double argmin_ms;     /* -1: the argmin is fused into the last path pass */
     double transfer_ms;   /* host<->device copies, kept apart from the phases */
     int    threads_used;  /* 0: not applicable on the GPU */

@@ -23,7 +23,7 @@
  *   SGMGB_MULTISCALE plans the frame loop of the standalone multi-scale
  *                         binary (multiscale/sgm_ms_ref.c:166-202).
  *   sgmgb_profile_frame   no reference symbol: per-kernel timing for the bench.
- *   sgmgb_set_path_shape, sgmgb_set_schedule
+ *   sgmgb_set_path_shape, sgmgb_set_schedule, sgmgb_alone_schedule
  *                         no reference symbol: speed knobs, results unchanged.
  *   sgmgb_batch_*         no reference symbol: many frames per launch.
  *   sgmgb_server_*        no reference symbol: a continuous-batching request loop.
@@ -114,12 +114,13 @@ int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane
  *               first halves of the rows run side by side with the vertical
  *               directions: the shortest critical path of the four. Same
  *               frames as FUSED; other frames run THROUGHPUT;
- *   AUTO        for sgmgb_run_frame and for a server frame with nothing
- *               else in flight: SPLIT on frames of at least 2,000,000 pixels
- *               at D >= 64 where it applies, LATENCY on the others; FUSED
- *               (THROUGHPUT where FUSED does not apply) for
- *               sgmgb_run_frame_async and the other server frames (the
- *               default).
+ *   AUTO        for sgmgb_run_frame: the schedule that runs fastest for a
+ *               frame alone, timed once per plan (sgmgb_alone_schedule tells
+ *               which); for a server frame with nothing else in flight: SPLIT
+ *               on frames of at least 2,000,000 pixels at D >= 64 where it
+ *               applies, LATENCY on the others; FUSED (THROUGHPUT where FUSED
+ *               does not apply) for sgmgb_run_frame_async and the other server
+ *               frames (the default).
  * Drops cached graphs. */
 #define SGMGB_SCHED_AUTO       0
 #define SGMGB_SCHED_LATENCY    1
@@ -127,14 +128,23 @@ int  sgmgb_set_path_shape(sgmgb_ctx *ctx, int warps_per_block, int disp_per_lane
 #define SGMGB_SCHED_FUSED      3
 #define SGMGB_SCHED_SPLIT      4
 int  sgmgb_set_schedule(sgmgb_ctx *ctx, int schedule);
+/* The schedule sgmgb_run_frame runs for the planned description: the set one,
+ * or under AUTO the fastest for a frame alone, timed on the first call after
+ * a plan or a shape or schedule change (this call makes that choice if no
+ * frame ran yet). */
+int  sgmgb_alone_schedule(sgmgb_ctx *ctx, int *schedule);
 
 /* ---- single frame ---- */
 /* Host buffers in and out, synchronous: the drop-in call. left/right are
- * W*H bytes, row-major; disp receives the output map (sgmgb_out_size).
- * Page-locked (or CUDA-registered) buffers are read and written across
- * NVLink-C2C by the kernels themselves; other host memory goes through the
- * copy engines. Under SGMGB_SCHED_AUTO it runs the schedule of a frame that
- * has the GPU to itself (SPLIT or LATENCY, above). */
+ * W*H bytes, row-major; disp receives the output map (sgmgb_out_size). The
+ * images are copied into the planned workspace by the copy engines (faster
+ * from page-locked or CUDA-registered memory), the frame runs as one CUDA
+ * graph with the schedule of sgmgb_alone_schedule, and the map is copied
+ * back. t (may be NULL): the frame's stage times, measured with CUDA events
+ * on the first call after a plan or a schedule or shape change and on every
+ * 8th call after it (the events cost about 3 us each), the latest measurement
+ * returned; census_ms, cost_ms and argmin_ms are -1 (one graph: aggregate_ms
+ * is the whole frame on the device). */
 int sgmgb_run_frame(sgmgb_ctx *ctx, const uint8_t *left, const uint8_t *right,
                     uint8_t *disp, sgmgb_stage_times *t);
 /* Device buffers, enqueued on `stream` (a cudaStream_t, NULL = the context's

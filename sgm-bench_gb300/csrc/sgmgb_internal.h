@@ -57,6 +57,17 @@ struct sgmgb_ctx {
     cudaGraphExec_t graph[kGraphs] = {};
     const void *graph_key[kGraphs][3] = {};
     int graph_next = 0;
+    // the synchronous call's frame: a CUDA graph on the slot's own buffers,
+    // with ev[1] and ev[2] recorded inside it, of the schedule that timed
+    // fastest for a frame alone (under AUTO; else the set schedule); made at
+    // the first sgmgb_run_frame after a plan or a shape change
+    cudaGraphExec_t alone = nullptr;
+    int alone_sched = 0;
+    // stage times of the synchronous call: measured on the first call after a
+    // plan and on every 8th call after it (each CUDA event on the stream costs
+    // about 3 us of a 0.38 ms frame), the latest measurement reported
+    unsigned timed_calls = 0;
+    sgmgb_stage_times last_times{-1, -1, -1, -1, -1, 0};
     PathShape shape;
     // optional post-steps (sgmgb_run_frame_post): their workspace, made on first use
     void *post = nullptr;

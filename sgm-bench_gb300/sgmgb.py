@@ -28,7 +28,7 @@ OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_NODEV, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE 
 EXPORTS = [
     "sgmgb_abi_version", "sgmgb_strerror", "sgmgb_last_error", "sgmgb_check_desc", "sgmgb_out_size",
     "sgmgb_workspace_bytes", "sgmgb_create", "sgmgb_destroy", "sgmgb_plan", "sgmgb_set_path_shape",
-    "sgmgb_set_schedule", "sgmgb_profile_frame",
+    "sgmgb_set_schedule", "sgmgb_alone_schedule", "sgmgb_profile_frame",
     "sgmgb_run_frame",
     "sgmgb_run_frame_async", "sgmgb_sync", "sgmgb_census_async", "sgmgb_batch_create", "sgmgb_batch_run",
     "sgmgb_batch_wait", "sgmgb_batch_autotune", "sgmgb_batch_tile_shape", "sgmgb_batch_set_fault",
@@ -93,6 +93,7 @@ def _load():
         "sgmgb_plan": (i, [vp, fdp]),
         "sgmgb_set_path_shape": (i, [vp, i, i]),
         "sgmgb_set_schedule": (i, [vp, i]),
+        "sgmgb_alone_schedule": (i, [vp, ctypes.POINTER(i)]),
         "sgmgb_profile_frame": (i, [vp, u8p, u8p, u8p, i, ctypes.POINTER(KernelStat), i, ctypes.POINTER(i)]),
         "sgmgb_run_frame": (i, [vp, u8p, u8p, u8p, ctypes.POINTER(StageTimes)]),
         "sgmgb_run_frame_async": (i, [vp, u8p, u8p, u8p, vp]),
@@ -247,6 +248,13 @@ class Engine:
         self._check(lib.sgmgb_set_schedule(self.h, schedule))
         return self
 
+    def alone_schedule(self):
+        """The schedule run_frame runs (SCHED_*): the set one, or under
+        SCHED_AUTO the one that timed fastest for a frame alone."""
+        v = ctypes.c_int()
+        self._check(lib.sgmgb_alone_schedule(self.h, ctypes.byref(v)))
+        return v.value
+
     def profile_frame(self, d_left, d_right, d_disp, reps=10):
         """Per-kernel mean device time (ms) and algorithmic bytes of the planned
         frame, every kernel timed alone with CUDA events: [(name, ms, bytes)]."""
@@ -259,7 +267,7 @@ class Engine:
     def run_frame(self, left, right, times=False, out=None):
         """Host arrays in, host disparity map out (the drop-in call). `out`: a
         C-contiguous uint8 array of the output size to fill (e.g. pinned memory,
-        which the kernels write directly), else a new array."""
+        which the copy back writes fastest), else a new array."""
         left = np.ascontiguousarray(left, np.uint8)
         right = np.ascontiguousarray(right, np.uint8)
         H, W = left.shape
@@ -274,7 +282,7 @@ class Engine:
             disp = out
         st = StageTimes()
         self._check(lib.sgmgb_run_frame(self.h, left.ctypes.data, right.ctypes.data, disp.ctypes.data,
-                                        ctypes.byref(st)))
+                                        ctypes.byref(st) if times else None))
         return (disp, st.as_dict()) if times else disp
 
     def run_frame_post(self, left, right, flags):

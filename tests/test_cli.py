@@ -169,7 +169,7 @@ def test_cli_plain_cost_gate(tmp_path):
             "--roofline-cal", cal)
     assert p.returncode == 0, p.stderr
     rows = [x.split() for x in open(cal).read().splitlines()]
-    assert {x[4] for x in rows} == {"census", "aggregate"}          # cost and argmin are fused (-1)
+    assert {x[4] for x in rows} == {"aggregate"}          # the frame is one graph: the other phases are -1
     assert all(x[:4] == ["gb300", "testbox", "320x200", "D64"] and float(x[5]) > 0 for x in rows)
     p = run("plain", tmp_path / "l.pgm", tmp_path / "r.pgm", "-n", 5, "--board", "testbox", "--roofline-cal", cal,
             "--roofline-max", 5, "-j", tmp_path / "a.jsonl")

@@ -193,8 +193,9 @@ def test_plugin_sgm_impl(D, paths):
         rc, disp, st = plug.run(left, right, threads=4)
         assert rc == 0
         assert np.array_equal(disp, oracle.plain(left, right, D, paths))
-    assert st["aggregate_ms"] >= 0 and st["census_ms"] >= 0 and st["transfer_ms"] >= 0
-    assert st["cost_ms"] == -1 and st["argmin_ms"] == -1 and st["threads_used"] == 0
+    assert st["aggregate_ms"] > 0 and st["transfer_ms"] >= 0
+    # the frame is one graph: its phases are one (aggregate), the fused ones -1
+    assert st["census_ms"] == -1 and st["cost_ms"] == -1 and st["argmin_ms"] == -1 and st["threads_used"] == 0
     rc, disp, st = plug.run(left[:100, :150], right[:100, :150])   # resolution change re-plans
     assert rc == 0 and np.array_equal(disp, oracle.plain(left[:100, :150], right[:100, :150], D, paths))
 
@@ -289,6 +290,32 @@ def test_auto_runs_split_for_a_large_frame_alone(engine):
         assert np.array_equal(ho, want)
         ho[:] = 0
     assert np.array_equal(engine.run_frame(left, right), want)         # pageable: through the copy engines
+
+
+def test_alone_schedule_is_timed_and_exact(engine):
+    """The synchronous call runs one CUDA graph with the schedule that timed
+    fastest for a frame alone (under AUTO) or the set one; every choice gives
+    the checker's map, and a new plan or schedule makes a new choice."""
+    import oracle
+    try:
+        for (W, H, D, paths, variant) in [(640, 480, 64, 4, sgmgb.PLAIN), (300, 200, 64, 8, sgmgb.MULTISCALE)]:
+            left, right, _ = sgmgb.synth_pair(W, H, D, seed=W + 3)
+            want = oracle.multiscale(left, right) if variant else oracle.plain(left, right, D, paths)
+            engine.set_schedule(sgmgb.SCHED_AUTO)
+            engine.plan(W, H, D, paths, variant)
+            allowed = {sgmgb.SCHED_LATENCY, sgmgb.SCHED_THROUGHPUT}
+            if not variant:
+                allowed |= {sgmgb.SCHED_FUSED, sgmgb.SCHED_SPLIT}
+            assert engine.alone_schedule() in allowed
+            assert np.array_equal(engine.run_frame(left, right), want)
+            for sched in sorted(allowed):
+                engine.set_schedule(sched)
+                assert engine.alone_schedule() == sched
+                got, st = engine.run_frame(left, right, times=True)
+                assert np.array_equal(got, want), (W, H, variant, sched)
+                assert st["census_ms"] == -1 and st["aggregate_ms"] > 0 and st["transfer_ms"] >= 0
+    finally:
+        engine.set_schedule(sgmgb.SCHED_AUTO)
 
 
 SCHEDS = {"latency": sgmgb.SCHED_LATENCY, "throughput": sgmgb.SCHED_THROUGHPUT, "fused": sgmgb.SCHED_FUSED,
