@@ -108,6 +108,10 @@ struct FrameSlot {
 
 namespace sgmgb {
 
+// Captures the frame on the slot's own buffers (inputs left/right, map disp)
+// under shape `sh` into a CUDA graph on stream st (which must be idle).
+cudaError_t capture_frame(const FrameSlot &s, cudaStream_t st, const PathShape &sh, cudaGraphExec_t *out);
+
 // Byte layout of a slot for a frame description; total in *bytes.
 size_t slot_layout(const sgmgb_frame_desc &fd, FrameSlot *s /* may be null: size only */);
 int  slot_alloc(const sgmgb_frame_desc &fd, FrameSlot **out, std::string &err);

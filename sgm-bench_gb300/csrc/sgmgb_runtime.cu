@@ -475,6 +475,20 @@ cudaError_t enqueue_frame(const FrameSlot &s, const uint8_t *d_left, const uint8
     return cudaSuccess;
 }
 
+cudaError_t capture_frame(const FrameSlot &s, cudaStream_t st, const PathShape &sh, cudaGraphExec_t *out) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t ee = enqueue_frame(s, s.left, s.right, s.disp, st, sh, nullptr, nullptr);
+    e = cudaStreamEndCapture(st, &g);
+    if (ee != cudaSuccess) { if (g) cudaGraphDestroy(g); return ee; }
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    return e;
+}
+
+
 }  // namespace sgmgb
 
 // ---------------------------------------------------------------------------
@@ -746,17 +760,7 @@ static void drop_graph(sgmgb_ctx *ctx) {
 // The frame on the slot's own buffers under schedule `sh`. (No stage event
 // inside: an event node in the graph measured 17 us slower per 1080p frame.)
 static cudaError_t capture_alone(sgmgb_ctx *ctx, const PathShape &sh, cudaGraphExec_t *out) {
-    const FrameSlot &s = *ctx->slot;
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    cudaError_t ee = enqueue_frame(s, s.left, s.right, s.disp, ctx->stream, sh, nullptr, nullptr);
-    e = cudaStreamEndCapture(ctx->stream, &g);
-    if (ee != cudaSuccess) { if (g) cudaGraphDestroy(g); return ee; }
-    if (e != cudaSuccess) return e;
-    e = cudaGraphInstantiate(out, g, 0);
-    cudaGraphDestroy(g);
-    return e;
+    return capture_frame(*ctx->slot, ctx->stream, sh, out);
 }
 
 // The synchronous call's graph. Under AUTO each schedule that applies to the
@@ -814,6 +818,7 @@ static cudaError_t alone_graph(sgmgb_ctx *ctx, cudaGraphExec_t *out) {
     *out = best;
     return cudaSuccess;
 }
+
 
 // Captures the frame pipeline for this pointer triple into a CUDA graph on
 // the context's stream (one graph launch per frame afterwards).

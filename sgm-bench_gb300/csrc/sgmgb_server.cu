@@ -46,7 +46,39 @@ struct Slot {
     FrameSlot *fs = nullptr;
     cudaStream_t st = nullptr;
     bool busy = false;
+    // the frame on this slot's buffers as CUDA graphs: [0] with frames in
+    // flight, [1] alone; captured when the slot is made (and again if the
+    // context's shape changed since), one launch per frame instead of a
+    // launch per kernel and fork on the dispatcher thread
+    cudaGraphExec_t g[2] = {nullptr, nullptr};
+    PathShape gsh[2];
 };
+
+bool same_shape(const PathShape &a, const PathShape &b) {
+    return a.sched == b.sched && a.wpb == b.wpb && a.dpl == b.dpl;
+}
+
+// The slot's graph for shape sh (captured on the slot's idle stream when
+// missing or stale), or null when the capture fails (no lock held).
+cudaGraphExec_t slot_graph(Slot &sl, const PathShape &sh, int which) {
+    if (sl.g[which] && same_shape(sl.gsh[which], sh)) return sl.g[which];
+    if (sl.g[which]) cudaGraphExecDestroy(sl.g[which]);
+    sl.g[which] = nullptr;
+    cudaGraphExec_t g = nullptr;
+    if (capture_frame(*sl.fs, sl.st, sh, &g) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    sl.g[which] = g;
+    sl.gsh[which] = sh;
+    return g;
+}
+
+void slot_release(Slot &sl) {
+    for (auto &g : sl.g) if (g) cudaGraphExecDestroy(g);
+    if (sl.st) { cudaStreamSynchronize(sl.st); cudaStreamDestroy(sl.st); }
+    slot_free(sl.fs);
+}
 
 struct Request {
     uint64_t ticket = 0;
@@ -120,9 +152,10 @@ size_t growth_bytes(const sgmgb_server *s, const Camera *c) {
     return s->resident + need <= s->cfg.hbm_budget_bytes ? need : 0;
 }
 
-// Allocates one slot (no lock held: CUDA calls only run without the lock, so a
-// completion callback waiting for the lock can never hold up a CUDA call).
-bool make_slot(const sgmgb_frame_desc &fd, Slot *out) {
+// Allocates one slot and captures its two frame graphs for `shape` (no lock
+// held: CUDA calls only run without the lock, so a completion callback
+// waiting for the lock can never hold up a CUDA call).
+bool make_slot(const sgmgb_frame_desc &fd, const PathShape &shape, Slot *out) {
     Slot sl;
     std::string err;
     if (slot_alloc(fd, &sl.fs, err) != SGMGB_OK) return false;
@@ -131,6 +164,7 @@ bool make_slot(const sgmgb_frame_desc &fd, Slot *out) {
         slot_free(sl.fs);
         return false;
     }
+    for (int which = 0; which < 2; which++) slot_graph(sl, resolve_sched(shape, which == 1, fd), which);
     *out = sl;
     return true;
 }
@@ -143,10 +177,12 @@ bool launch(sgmgb_server *s, Request *r, int k, bool alone, std::string &err) {
     Slot &sl = c->slots[k];
     const FrameSlot &fs = *sl.fs;
     uint8_t *hb = c->bufs[r->buf];
+    const PathShape sh = resolve_sched(s->ctx->shape, alone, fs.fd);
+    cudaGraphExec_t g = slot_graph(sl, sh, alone ? 1 : 0);   // before the copies: the stream is idle
     cudaError_t e = cudaMemcpyAsync(fs.left, hb, c->n_in, cudaMemcpyHostToDevice, sl.st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fs.right, hb + c->n_in, c->n_in, cudaMemcpyHostToDevice, sl.st);
     if (e == cudaSuccess)
-        e = enqueue_frame(fs, fs.left, fs.right, fs.disp, sl.st, resolve_sched(s->ctx->shape, alone, fs.fd), nullptr, nullptr);
+        e = g ? cudaGraphLaunch(g, sl.st) : enqueue_frame(fs, fs.left, fs.right, fs.disp, sl.st, sh, nullptr, nullptr);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hb + 2 * c->n_in, fs.disp, c->n_out, cudaMemcpyDeviceToHost, sl.st);
     if (e == cudaSuccess) e = cudaLaunchHostFunc(sl.st, on_frame_done, r);
     if (e != cudaSuccess) {
@@ -225,7 +261,7 @@ void worker_main(sgmgb_server *s) {
             std::string err;
             if (a.slot < 0) {
                 Slot sl;
-                if (!make_slot(c->fd, &sl)) {
+                if (!make_slot(c->fd, s->ctx->shape, &sl)) {
                     failed.push_back({a, "server: slot allocation failed"});
                     continue;
                 }
@@ -329,7 +365,7 @@ int sgmgb_server_add_camera(sgmgb_server *s, int cam_id, const sgmgb_frame_desc 
     }
     cudaSetDevice(s->ctx->device);
     Slot first;
-    if (!make_slot(*fd, &first)) {
+    if (!make_slot(*fd, s->ctx->shape, &first)) {
         std::lock_guard<std::mutex> g(s->mu);
         s->resident -= need;
         s->adding.erase(cam_id);
@@ -348,8 +384,7 @@ int sgmgb_server_add_camera(sgmgb_server *s, int cam_id, const sgmgb_frame_desc 
     }
     c->buf_used.assign(c->bufs.size(), false);
     if (c->bufs.empty()) {
-        cudaStreamDestroy(first.st);
-        slot_free(first.fs);
+        slot_release(first);
         std::lock_guard<std::mutex> g(s->mu);
         s->resident -= need;
         s->adding.erase(cam_id);
@@ -384,7 +419,7 @@ int sgmgb_server_prepare(sgmgb_server *s, int slots_per_camera, int *slots_resid
         }
         for (auto &t : todo) {
             Slot sl;
-            const bool ok = make_slot(t.first->fd, &sl);
+            const bool ok = make_slot(t.first->fd, s->ctx->shape, &sl);
             std::lock_guard<std::mutex> g(s->mu);
             t.first->growing--;
             if (!ok) { s->resident -= t.second; continue; }
@@ -498,10 +533,7 @@ void sgmgb_server_destroy(sgmgb_server *s) {
     cudaSetDevice(s->ctx->device);
     for (auto &kv : s->cams) {
         Camera *c = kv.second;
-        for (Slot &sl : c->slots) {
-            if (sl.st) { cudaStreamSynchronize(sl.st); cudaStreamDestroy(sl.st); }
-            slot_free(sl.fs);
-        }
+        for (Slot &sl : c->slots) slot_release(sl);
         for (uint8_t *p : c->bufs) cudaFreeHost(p);
         delete c;
     }
