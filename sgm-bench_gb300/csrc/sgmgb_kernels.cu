@@ -17,8 +17,8 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? l
 // code is in sgmgb_tiles.cuh.
 // ---------------------------------------------------------------------------
 // Tiles of CEN_FRAME_ROWS rows: 1.5 image bytes staged per pixel against 2.2
-// with 8-row tiles, which matters when the images are read across NVLink-C2C
-// from page-locked host memory.
+// with 8-row tiles (the kernel also reads images from page-locked host memory
+// across NVLink-C2C when handed such a pointer).
 constexpr int CEN_FRAME_ROWS = 32;
 
 __global__ void __launch_bounds__(256)

@@ -109,8 +109,7 @@ __device__ __forceinline__ void census_tile(const uint8_t *__restrict__ im, uint
     if ((W & 15) == 0 && ((uintptr_t)im & 15) == 0 && x0 >= 16 && x0 + CEN_PX + 16 <= W) {
         // interior tile: 16-byte loads of image bytes [x0-16, x0+CEN_PX+16) per
         // row (word j of the row's loads holds tile words 4j-3 .. 4j); a tenth
-        // of the loads of byte staging, which matters most when the image is
-        // read across NVLink-C2C from host memory
+        // of the loads of byte staging
         constexpr int VPR = (CEN_PX + 32) / 16;       // 16-byte loads per tile row
         for (int i = tid; i < CEN_TH * VPR; i += nthreads) {
             const int ty = i / VPR, j = i - ty * VPR;

@@ -265,10 +265,10 @@ def test_profile_frame_lists_every_kernel(engine):
 
 
 def test_auto_runs_split_for_a_large_frame_alone(engine):
-    """Under AUTO a frame alone of at least 2 Mpixel at D >= 64 takes the split
-    schedule (the profile lists its kernels), and the synchronous call, whose
-    last passes write the map straight into page-locked host memory, returns
-    the checker's map."""
+    """Under AUTO the profile of a frame of at least 2 Mpixel at D >= 64 lists
+    the split schedule's kernels (the schedule of a server frame alone), and
+    the synchronous call (its own timed choice) returns the checker's map on
+    page-locked and on pageable buffers."""
     import torch
     from conftest import reference_plain
     W, H, D = 1920, 1080, 64
