@@ -57,10 +57,10 @@ struct sgmgb_ctx {
     cudaGraphExec_t graph[kGraphs] = {};
     const void *graph_key[kGraphs][3] = {};
     int graph_next = 0;
-    // the synchronous call's frame: a CUDA graph on the slot's own buffers,
-    // with ev[1] and ev[2] recorded inside it, of the schedule that timed
-    // fastest for a frame alone (under AUTO; else the set schedule); made at
-    // the first sgmgb_run_frame after a plan or a shape change
+    // the synchronous call's frame: a CUDA graph on the slot's own buffers, of
+    // the schedule that timed fastest for a frame alone (under AUTO; else the
+    // set schedule); made at the first sgmgb_run_frame after a plan or a shape
+    // change
     cudaGraphExec_t alone = nullptr;
     int alone_sched = 0;
     // stage times of the synchronous call: measured on the first call after a

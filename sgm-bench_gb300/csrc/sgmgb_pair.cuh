@@ -241,14 +241,26 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
     uint32_t dpk[NR];                                 // (d, d) for the argmin keys
 #pragma unroll
     for (int j = 0; j < NR; j++) dpk[j] = pk2((uint32_t)(lane * NR + j));
+    // even-only scratch: the steps whose pixels are stored (x and y both even)
+    // alternate; when both lines agree on which (a chunk is an even number of
+    // steps), the others skip staging their L bytes
+    int eoph = -1;
+    if (MODE == MODE_SCRATCH && SAT != 0 && P.even_only) {
+        const int pha = (xa | ya) & 1, phb = lenb ? (xb | yb) & 1 : pha;
+        if (pha == phb) eoph = pha;
+    }
     pa -= step; pb -= step; xa -= dx; ya -= dy; xb -= dx; yb -= dy;
     const int hw = P.W >> 1;
 
     uint32_t dacc[2][KW] = {};                        // FINAL3H: the chunk's disparities of rows A and B, byte k = step k
     // one step of both lines; `row`: this step's cost row in the chunk; kk: the step within the chunk
+    // EO (even-only scratch, saturating passes only): -1 stage every step's L;
+    // 0 (1) stage the even (odd) steps of a chunk only, the others' pixels
+    // being odd and never stored
     auto step_once = [&](const uint32_t (&c)[NR], const uint32_t (&ps)[NR], const uint32_t (&sv)[NR], uint8_t *row,
-                         int i, int kk, auto full_t) {
+                         int i, int kk, auto full_t, auto eo_t) {
         constexpr bool FULL = decltype(full_t)::value;
+        constexpr int EO = decltype(eo_t)::value;
         if (!FULL && i >= maxlen) return;             // past both lines' ends (warp-uniform): L and mn stay
         pa += step; pb += step; xa += dx; ya += dy; xb += dx; yb += dy;
         const uint32_t up = __shfl_up_sync(kFull, L[NR - 1], 1) | mlo;
@@ -277,6 +289,7 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
         mn = __byte_perm(ra, rb, 0x7610);
         const bool live_a = FULL ? true : i < lena, live_b = FULL ? lenb > 0 : i < lenb;
         if (MODE == MODE_SCRATCH) {
+            if (EO >= 0 && (kk & 1) != EO) return;    // even-only: this step's pixels are not stored
             // stage both lines' L bytes in the consumed cost row of this step
             st_run<NR>(row + lane * NR, pair_pack<NR, false>(L));
             st_run<NR>(row + D + lane * NR, pair_pack<NR, true>(L));
@@ -394,12 +407,23 @@ __device__ __forceinline__ void path_pair(const LineParams &P, int warp, uint8_t
 #pragma unroll
             for (int w = 0; w < KW; w++) dacc[0][w] = dacc[1][w] = 0u;
         }
-        if ((ch + 1) * K <= minlen) {
+        auto steps = [&](auto eo_t) {
+            if ((ch + 1) * K <= minlen) {
 #pragma unroll
-            for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, k, std::true_type{});
+                for (int k = 0; k < K; k++)
+                    step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, k, std::true_type{}, eo_t);
+            } else {
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, k, std::false_type{}, eo_t);
+            }
+        };
+        if constexpr (MODE == MODE_SCRATCH && SAT != 0) {
+            if (eoph == 0) steps(std::integral_constant<int, 0>{});
+            else if (eoph == 1) steps(std::integral_constant<int, 1>{});
+            else steps(std::integral_constant<int, -1>{});
         } else {
-#pragma unroll
-            for (int k = 0; k < K; k++) step_once(c[k], ps[k], sv[k], chunk + k * SB, ch * K + k, k, std::false_type{});
+            steps(std::integral_constant<int, -1>{});
         }
         if (MODE == MODE_FINAL3H && lane == 0) {
             // row r's live steps of the chunk go to disp[p0 + dx*k]: one word store per 4 steps
