@@ -184,19 +184,30 @@ def batched_section(eng_cls, sgmgb, torch, np):
     eng = eng_cls(0)
     b = sgmgb.Batch(eng, [sgmgb.desc(*sp) for sp in specs])
     b.autotune(dl, dr, out)
-    b.run(dl, dr, out)
-    b.wait()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 5
-    s = torch.cuda.current_stream()
-    e0.record(s)
-    for _ in range(reps):
-        b.run(dl, dr, out, stream=s)           # on the stream the events are recorded on
-    e1.record(s)
-    b.wait()
-    torch.cuda.synchronize()
-    batch_ms = e0.elapsed_time(e1) / reps
+    mode, lanes = b.mode()
+
+    def time_batch():
+        b.run(dl, dr, out)
+        b.wait()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5
+        s = torch.cuda.current_stream()
+        e0.record(s)
+        for _ in range(reps):
+            b.run(dl, dr, out, stream=s)           # on the stream the events are recorded on
+        e1.record(s)
+        b.wait()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # both modes, the autotuned one last (its maps are the ones checked)
+    other = (sgmgb.BATCH_IN_FLIGHT, 6) if mode == sgmgb.BATCH_PERSISTENT else (sgmgb.BATCH_PERSISTENT, 0)
+    b.set_mode(*other)
+    other_ms = time_batch()
+    b.set_mode(mode, lanes or 6)
+    batch_ms = time_batch()
+    mode_ms = {mode: batch_ms, other[0]: other_ms}
     engs = {sp: eng_cls(0).plan(*sp) for sp in set(specs)}
     ref = [engs[sp].run_frame(l, r) for sp, (l, r) in zip(specs, host)]        # warm-up and reference maps
     t0 = time.perf_counter()
@@ -231,13 +242,17 @@ def batched_section(eng_cls, sgmgb, torch, np):
             "block_time_ms": {k: round(v, 3) for k, v in busy_ms.items()},
             "block_time_share": {k: round(v / max(1e-9, sum(busy_ms.values())), 4) for k, v in busy_ms.items()},
             "blocks": blocks,
-            "busy_per_block_over_run": sum(busy_ms.values()) / blocks / batch_ms,
+            "busy_per_block_over_run": sum(busy_ms.values()) / blocks / mode_ms[sgmgb.BATCH_PERSISTENT],
             "block_time_note": "time the persistent kernel's blocks spent per work-item kind in the last run "
                                "(global-timer stamps, summed over blocks); 'wait' is time "
                                "spent waiting for an item's inputs or on an empty queue",
-            "launches_per_batch": 1, "tile_shapes_warps_dpl": shapes,
-            "note": "one persistent launch per batch (CUDA graph); batch inputs resident on the device; "
-                    "drop-in calls copy host buffers in and out"}, checks
+            "mode": "in_flight" if mode == sgmgb.BATCH_IN_FLIGHT else "persistent", "lanes": lanes,
+            "persistent_ms": mode_ms[sgmgb.BATCH_PERSISTENT], "in_flight_ms": mode_ms[sgmgb.BATCH_IN_FLIGHT],
+            "tile_shapes_warps_dpl": shapes,
+            "note": "the mode the autotuner kept: one persistent launch per batch, or every frame's own "
+                    "pipeline on concurrent chains (in_flight, 6 lanes timed for the other figure), each a "
+                    "CUDA graph per batch; block time is the persistent launch's; batch inputs resident on "
+                    "the device; drop-in calls copy host buffers in and out"}, checks
 
 
 def served_section(eng_cls, sgmgb, np, rates=(2000.0, 3000.0, 4000.0), secs=3.0):

@@ -224,9 +224,10 @@ int sgmgb_census_async(sgmgb_ctx *ctx, const uint8_t *d_img, uint64_t *d_out, in
 int sgmgb_run_frame_noalloc(const uint8_t *d_left, const uint8_t *d_right, uint8_t *d_disp,
                             int W, int H, int D, int paths, void *stream);
 
-/* ---- batch: many frames of mixed sizes in one persistent launch ---- */
+/* ---- batch: many frames of mixed sizes in one run ---- */
 /* A batch runs n plain-variant frames of any sizes, disparity ranges and path
- * counts in ONE persistent kernel launch: its blocks take work items (census
+ * counts in ONE persistent kernel launch (or as frames in flight: see
+ * sgmgb_batch_set_mode): its blocks take work items (census
  * row bands, cost row bands, groups of lines of one direction) from a device
  * queue in phase order and wait, with a bounded spin, on per-frame phase
  * counters. The launch and its counter resets are captured in a CUDA graph on
@@ -251,21 +252,24 @@ int  sgmgb_batch_run(sgmgb_batch *b, const uint8_t *const *d_left,
  * wait for its inputs ran past the wait limit (the run was abandoned and the
  * outputs are undefined; the context stays usable). */
 int  sgmgb_batch_wait(sgmgb_batch *b);
-/* Times candidate shapes (warps per block 2 and 4; disparities per lane 0 --
- * the two-lines-per-warp layout --, the smallest valid, and twice that) on
- * these buffers, keeps the fastest, and, when tune_cache is not NULL, records
- * it for every frame description. */
+/* Times candidate shapes of the persistent launch (warps per block 2 and 4;
+ * disparities per lane 0 -- the two-lines-per-warp layout --, the smallest
+ * valid, and twice that) on these buffers, keeps the fastest, and, when
+ * tune_cache is not NULL, records it for every frame description; then times
+ * the frames-in-flight mode (SGMGB_BATCH_IN_FLIGHT below) on 4, 6 and 8
+ * lanes and keeps the faster mode. */
 int  sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left,
                           const uint8_t *const *d_right, uint8_t *const *d_disp,
                           const char *tune_cache);
-/* Where the last run's time went (no reference symbol): ms[k] is the time
- * the persistent kernel's blocks spent on work items of kind k, summed over
- * blocks, in milliseconds of the GPU's global timer: k = 0 census, 1 cost,
+/* Where the last persistent launch's time went (no reference symbol): ms[k]
+ * is the time the persistent kernel's blocks spent on work items of kind k,
+ * summed over blocks, in milliseconds of the GPU's global timer: k = 0 census, 1 cost,
  * 2 passes that park a direction's L, 3 final passes (planes added, argmin),
  * 4 first halves of split rows with their costs, 5 waiting for an item's
  * inputs (or for the queue to end). n <= 6 entries are filled (more are set
  * to 0); *blocks (may be NULL) receives the launch's block count, so that
- * sum(ms) / blocks is about the run's time. Waits for the last run. */
+ * sum(ms) / blocks is about the launch's time. Waits for the last run;
+ * SGMGB_ERR_STATE before the first persistent launch. */
 int  sgmgb_batch_busy(sgmgb_batch *b, double *ms, int n, int *blocks);
 /* Path-kernel shape used for frame i: warps per block and disparities per lane. */
 int  sgmgb_batch_tile_shape(const sgmgb_batch *b, int i, int *warps_per_block,
@@ -276,6 +280,26 @@ int  sgmgb_batch_tile_shape(const sgmgb_batch *b, int i, int *warps_per_block,
  * items wait until the limit and the next run reports SGMGB_ERR_TIMEOUT.
  * stall_frame = -1 clears it. */
 int  sgmgb_batch_set_fault(sgmgb_batch *b, int wait_limit_ms, int stall_frame);
+/* How sgmgb_batch_run executes the planned frames (no reference symbol;
+ * outputs never change):
+ *   SGMGB_BATCH_PERSISTENT  the one persistent launch above (after create);
+ *   SGMGB_BATCH_IN_FLIGHT   every frame's own pipeline, as
+ *                           sgmgb_run_frame_async runs it with frames in
+ *                           flight (the fused schedule where it applies, else
+ *                           the throughput one; 4 warps per block, the
+ *                           smallest disparities per lane), on `lanes` (1..8)
+ *                           concurrent chains of about equal work (frames
+ *                           largest first, each onto the least loaded chain);
+ *                           the whole run is one CUDA graph, captured again
+ *                           when the device pointers differ from the last run's.
+ * Runs of either mode on one stream are ordered. The wait limit and the
+ * stall of sgmgb_batch_set_fault, and sgmgb_batch_busy, concern the
+ * persistent launch. sgmgb_batch_autotune times both modes and keeps the
+ * faster (lanes 4, 6 and 8 for the second). */
+#define SGMGB_BATCH_PERSISTENT 0
+#define SGMGB_BATCH_IN_FLIGHT  1
+int  sgmgb_batch_set_mode(sgmgb_batch *b, int mode, int lanes);
+int  sgmgb_batch_mode(const sgmgb_batch *b, int *mode, int *lanes);
 void sgmgb_batch_destroy(sgmgb_batch *b);
 
 /* ---- autotuner cache (host-only; no GPU needed) ---- */

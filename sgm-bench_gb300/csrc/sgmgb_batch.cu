@@ -1,4 +1,5 @@
-// sgmgb_batch.cu -- many frames of mixed sizes in one persistent launch.
+// sgmgb_batch.cu -- many frames of mixed sizes in one persistent launch (or as
+// frames in flight in one CUDA graph: SGMGB_BATCH_IN_FLIGHT, at the end).
 //
 // Work decomposition (plain variant, common/sgm_ref.c semantics per frame):
 //   phase 0  census   one item per band of BAND (8) rows (both images)
@@ -344,6 +345,20 @@ struct sgmgb_batch {
     bool ran = false;
     int wait_limit_ms = 2000;
     int stall_frame = -1;
+    // frames in flight (SGMGB_BATCH_IN_FLIGHT): each frame's own pipeline on
+    // one of `lanes` chains; a chain is a stream plus the forked streams and events
+    // of its frames (FrameSlot fields, no buffers); the run is one graph,
+    // keyed by the device pointers it was captured with
+    int mode = SGMGB_BATCH_PERSISTENT;
+    int lanes = 0;
+    std::vector<FrameSlot> chain;
+    std::vector<cudaStream_t> chain_st;
+    cudaEvent_t lane_fork = nullptr;
+    std::vector<cudaEvent_t> lane_join;
+    cudaGraphExec_t fgraph = nullptr;
+    std::vector<const void *> fkey;
+    bool last_persistent = false;         // the last run was the persistent launch
+    bool ran_persistent = false;          // h_ctl[1] holds a persistent launch's read-back
 };
 
 namespace {
@@ -528,6 +543,117 @@ int capture_graph(sgmgb_batch *b) {
     return SGMGB_OK;
 }
 
+void free_lanes(sgmgb_batch *b) {
+    if (b->fgraph) { cudaGraphExecDestroy(b->fgraph); b->fgraph = nullptr; }
+    b->fkey.clear();
+    for (FrameSlot &c : b->chain) {
+        for (auto &a : c.aux) if (a) cudaStreamDestroy(a);
+        if (c.fork) cudaEventDestroy(c.fork);
+        for (auto &j : c.join) if (j) cudaEventDestroy(j);
+    }
+    b->chain.clear();
+    for (cudaStream_t s : b->chain_st) if (s) cudaStreamDestroy(s);
+    b->chain_st.clear();
+    for (cudaEvent_t e : b->lane_join) if (e) cudaEventDestroy(e);
+    b->lane_join.clear();
+    if (b->lane_fork) { cudaEventDestroy(b->lane_fork); b->lane_fork = nullptr; }
+    b->lanes = 0;
+}
+
+// The streams and events of `lanes` chains (kept while the count stays).
+int make_lanes(sgmgb_batch *b, int lanes) {
+    if (b->lanes == lanes) return SGMGB_OK;
+    free_lanes(b);
+    b->chain.resize(lanes);
+    b->chain_st.assign(lanes, nullptr);
+    b->lane_join.assign(lanes, nullptr);
+    b->lanes = lanes;
+    cudaError_t e = cudaEventCreateWithFlags(&b->lane_fork, cudaEventDisableTiming);
+    for (int k = 0; k < lanes && e == cudaSuccess; k++) {
+        FrameSlot &c = b->chain[k];
+        e = cudaStreamCreateWithFlags(&b->chain_st[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->lane_join[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming);
+        for (int i = 0; i < FrameSlot::kAux && e == cudaSuccess; i++) {
+            e = cudaStreamCreateWithFlags(&c.aux[i], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.join[i], cudaEventDisableTiming);
+        }
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        free_lanes(b);
+        return berr(b, SGMGB_ERR_CUDA, std::string("batch lanes: ") + cudaGetErrorString(e));
+    }
+    return SGMGB_OK;
+}
+
+// Captures the frames-in-flight run on these buffers: a fork from the
+// capture stream to every chain, each frame's pipeline (enqueue_frame, as
+// sgmgb_run_frame_async with frames in flight runs it) on its chain, and the
+// chains' joins.
+int capture_lanes(sgmgb_batch *b, const uint8_t *const *dl, const uint8_t *const *dr, uint8_t *const *dd) {
+    if (b->fgraph) {
+        if (b->ran) cudaEventSynchronize(b->done_ev);   // the graph may be running
+        cudaGraphExecDestroy(b->fgraph);
+        b->fgraph = nullptr;
+    }
+    b->fkey.clear();
+    cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { cudaGetLastError(); return berr(b, SGMGB_ERR_CUDA, "batch capture"); }
+    e = cudaEventRecord(b->lane_fork, b->cap);
+    for (int k = 0; k < b->lanes && e == cudaSuccess; k++) e = cudaStreamWaitEvent(b->chain_st[k], b->lane_fork, 0);
+    PathShape sh;
+    sh.sched = SGMGB_SCHED_FUSED;                     // the throughput schedule where it does not apply
+    // chains of about equal work: frames largest first, each onto the chain
+    // with the least work so far (work ~ W*H*D, 8 paths counted 1.8 times)
+    std::vector<int> order(b->n);
+    std::vector<double> work(b->n), load(b->lanes, 0.0);
+    for (int f = 0; f < b->n; f++) {
+        const sgmgb_frame_desc &fd = b->fds[f];
+        order[f] = f;
+        work[f] = (double)fd.W * fd.H * fd.D * (fd.paths == 8 ? 1.8 : 1.0);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return work[a] > work[c]; });
+    for (int f : order) {
+        if (e != cudaSuccess) break;
+        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += work[f];
+        FrameSlot v = b->slots[f];                    // the frame's buffers, its chain's streams
+        const FrameSlot &c = b->chain[k];
+        std::copy(c.aux, c.aux + FrameSlot::kAux, v.aux);
+        std::copy(c.join, c.join + FrameSlot::kAux, v.join);
+        v.fork = c.fork;
+        e = enqueue_frame(v, dl[f], dr[f], dd[f], b->chain_st[k], sh, nullptr, nullptr);
+    }
+    for (int k = 0; k < b->lanes && e == cudaSuccess; k++) {
+        e = cudaEventRecord(b->lane_join[k], b->chain_st[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->cap, b->lane_join[k], 0);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(b->cap, &g);
+    if (e == cudaSuccess) e = ee;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->fgraph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b->fgraph = nullptr;
+        return berr(b, SGMGB_ERR_CUDA, std::string("batch frames graph: ") + cudaGetErrorString(e));
+    }
+    for (int f = 0; f < b->n; f++) {
+        b->fkey.push_back(dl[f]);
+        b->fkey.push_back(dr[f]);
+        b->fkey.push_back(dd[f]);
+    }
+    return SGMGB_OK;
+}
+
+bool same_key(const sgmgb_batch *b, const uint8_t *const *dl, const uint8_t *const *dr, uint8_t *const *dd) {
+    if (b->fkey.size() != (size_t)3 * b->n) return false;
+    for (int f = 0; f < b->n; f++)
+        if (b->fkey[3 * f] != dl[f] || b->fkey[3 * f + 1] != dr[f] || b->fkey[3 * f + 2] != dd[f]) return false;
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -599,14 +725,25 @@ int sgmgb_batch_run(sgmgb_batch *b, const uint8_t *const *d_left, const uint8_t 
     for (int f = 0; f < b->n; f++)
         if (!d_left[f] || !d_right[f] || !d_disp[f]) return berr(b, SGMGB_ERR_ARG, "batch frame " + std::to_string(f) + ": null buffer");
     cudaSetDevice(b->ctx->device);
-    if (b->ran) cudaEventSynchronize(b->done_ev);   // the pinned table is read by the previous run
-    fill_frames(b, d_left, d_right, d_disp);
-    if (!b->graph) {
-        const int rc = capture_graph(b);
-        if (rc) return rc;
-    }
     cudaStream_t st = stream ? (cudaStream_t)stream : b->ctx->stream;
-    cudaError_t e = cudaGraphLaunch(b->graph, st);
+    cudaError_t e;
+    if (b->mode == SGMGB_BATCH_IN_FLIGHT) {
+        if (!b->fgraph || !same_key(b, d_left, d_right, d_disp)) {
+            const int rc = capture_lanes(b, d_left, d_right, d_disp);
+            if (rc) return rc;
+        }
+        e = cudaGraphLaunch(b->fgraph, st);
+        b->last_persistent = false;
+    } else {
+        if (b->ran) cudaEventSynchronize(b->done_ev);   // the pinned table is read by the previous run
+        fill_frames(b, d_left, d_right, d_disp);
+        if (!b->graph) {
+            const int rc = capture_graph(b);
+            if (rc) return rc;
+        }
+        e = cudaGraphLaunch(b->graph, st);
+        b->last_persistent = b->ran_persistent = true;
+    }
     if (e == cudaSuccess) e = cudaEventRecord(b->done_ev, st);
     if (e != cudaSuccess) { cudaGetLastError(); return berr(b, SGMGB_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e)); }
     b->ran = true;
@@ -619,7 +756,7 @@ int sgmgb_batch_wait(sgmgb_batch *b) {
     cudaSetDevice(b->ctx->device);
     cudaError_t e = cudaEventSynchronize(b->done_ev);
     if (e != cudaSuccess) { cudaGetLastError(); return berr(b, SGMGB_ERR_CUDA, std::string("batch run: ") + cudaGetErrorString(e)); }
-    if (b->h_ctl[1].err_item != -1)
+    if (b->last_persistent && b->h_ctl[1].err_item != -1)
         return berr(b, SGMGB_ERR_TIMEOUT, "batch item " + std::to_string(b->h_ctl[1].err_item) + " waited past " +
                                               std::to_string(b->wait_limit_ms) + " ms for its inputs; run abandoned");
     return SGMGB_OK;
@@ -629,7 +766,7 @@ int sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left, const uin
                          uint8_t *const *d_disp, const char *tune_cache) {
     if (!b) return SGMGB_ERR_ARG;
     cudaSetDevice(b->ctx->device);
-    const int saved_wpb = b->wpb;
+    const int saved_wpb = b->wpb, saved_mode = b->mode, saved_lanes = b->lanes;
     const std::vector<int> saved_dpl = b->dpl;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess) {
@@ -637,42 +774,67 @@ int sgmgb_batch_autotune(sgmgb_batch *b, const uint8_t *const *d_left, const uin
         if (t0) cudaEventDestroy(t0);
         return berr(b, SGMGB_ERR_CUDA, "autotune events");
     }
-    float best = -1.f;
-    int best_w = saved_wpb, best_m = 0, rc = SGMGB_OK;
+    // one untimed run (capture, warm-up), then the best of three on the context's stream
+    auto time_runs = [&](float *ms) -> int {
+        int r;
+        if ((r = sgmgb_batch_run(b, d_left, d_right, d_disp, nullptr)) || (r = sgmgb_batch_wait(b))) return r;
+        *ms = 1e30f;
+        for (int rep = 0; rep < 3; rep++) {
+            cudaEventRecord(t0, b->ctx->stream);
+            if ((r = sgmgb_batch_run(b, d_left, d_right, d_disp, nullptr))) return r;
+            cudaEventRecord(t1, b->ctx->stream);
+            if ((r = sgmgb_batch_wait(b))) return r;
+            float t = 0.f;
+            cudaEventElapsedTime(&t, t0, t1);
+            *ms = std::min(*ms, t);
+        }
+        return SGMGB_OK;
+    };
+    float best = -1.f, best_flight = -1.f;
+    int best_w = saved_wpb, best_m = 0, best_lanes = 0, rc = SGMGB_OK;
     auto shape_of = [&](int f, int m) {   // m = 0: pair layout; 1, 2: smallest valid and twice that
         return m ? path_dpl(b->fds[f].D, std::min(8, path_dpl(b->fds[f].D, 0) * m)) : 0;
     };
+    b->mode = SGMGB_BATCH_PERSISTENT;
     for (int w : {2, 4}) {
         for (int m : {0, 1, 2}) {
+            if (rc) break;
             b->wpb = w;
             for (int f = 0; f < b->n; f++) b->dpl[f] = shape_of(f, m);
-            if ((rc = build_plan(b))) goto done;
-            if ((rc = sgmgb_batch_run(b, d_left, d_right, d_disp, nullptr)) || (rc = sgmgb_batch_wait(b))) goto done;
-            float ms = 1e30f;
-            for (int rep = 0; rep < 3; rep++) {
-                cudaEventRecord(t0, b->ctx->stream);
-                if ((rc = sgmgb_batch_run(b, d_left, d_right, d_disp, nullptr))) goto done;
-                cudaEventRecord(t1, b->ctx->stream);
-                if ((rc = sgmgb_batch_wait(b))) goto done;
-                float t = 0.f;
-                cudaEventElapsedTime(&t, t0, t1);
-                ms = std::min(ms, t);
-            }
+            float ms = 0.f;
+            if ((rc = build_plan(b)) || (rc = time_runs(&ms))) break;
             if (best < 0.f || ms < best) { best = ms; best_w = w; best_m = m; }
         }
     }
-done:
+    if (!rc) {
+        b->wpb = best_w;
+        for (int f = 0; f < b->n; f++) b->dpl[f] = shape_of(f, best_m);
+        rc = build_plan(b);
+    }
+    // frames in flight (shapes of their own: the persistent launch's do not apply)
+    b->mode = SGMGB_BATCH_IN_FLIGHT;
+    for (int lanes : {4, 6, 8}) {
+        if (rc) break;
+        float ms = 0.f;
+        if ((rc = make_lanes(b, lanes)) || (rc = time_runs(&ms))) break;
+        if (best_flight < 0.f || ms < best_flight) { best_flight = ms; best_lanes = lanes; }
+    }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     if (rc) {
         b->wpb = saved_wpb;
         b->dpl = saved_dpl;
         build_plan(b);
+        b->mode = saved_mode;
+        if (saved_mode == SGMGB_BATCH_IN_FLIGHT) make_lanes(b, saved_lanes);
         return rc;
     }
-    b->wpb = best_w;
-    for (int f = 0; f < b->n; f++) b->dpl[f] = shape_of(f, best_m);
-    if ((rc = build_plan(b))) return rc;
+    if (best_flight < best) {
+        b->mode = SGMGB_BATCH_IN_FLIGHT;
+        if ((rc = make_lanes(b, best_lanes))) return rc;
+    } else {
+        b->mode = SGMGB_BATCH_PERSISTENT;
+    }
     if (tune_cache) {
         for (int f = 0; f < b->n; f++) {
             bool seen = false;
@@ -686,7 +848,7 @@ done:
 
 int sgmgb_batch_busy(sgmgb_batch *b, double *ms, int n, int *blocks) {
     if (!b || !ms || n < 1) return SGMGB_ERR_ARG;
-    if (!b->ran) return berr(b, SGMGB_ERR_STATE, "the batch has not run");
+    if (!b->ran_persistent) return berr(b, SGMGB_ERR_STATE, "the persistent launch has not run");
     cudaSetDevice(b->ctx->device);
     if (cudaEventSynchronize(b->done_ev) != cudaSuccess) {
         cudaGetLastError();
@@ -704,6 +866,26 @@ int sgmgb_batch_tile_shape(const sgmgb_batch *b, int i, int *warps_per_block, in
     return SGMGB_OK;
 }
 
+int sgmgb_batch_set_mode(sgmgb_batch *b, int mode, int lanes) {
+    if (!b || (mode != SGMGB_BATCH_PERSISTENT && mode != SGMGB_BATCH_IN_FLIGHT)) return SGMGB_ERR_ARG;
+    if (mode == SGMGB_BATCH_IN_FLIGHT && (lanes < 1 || lanes > 8)) return SGMGB_ERR_ARG;
+    cudaSetDevice(b->ctx->device);
+    if (mode == SGMGB_BATCH_IN_FLIGHT && lanes != b->lanes) {
+        if (b->ran) cudaEventSynchronize(b->done_ev);  // the frames graph may be running
+        const int rc = make_lanes(b, lanes);
+        if (rc) return rc;
+    }
+    b->mode = mode;
+    return SGMGB_OK;
+}
+
+int sgmgb_batch_mode(const sgmgb_batch *b, int *mode, int *lanes) {
+    if (!b) return SGMGB_ERR_ARG;
+    if (mode) *mode = b->mode;
+    if (lanes) *lanes = b->mode == SGMGB_BATCH_IN_FLIGHT ? b->lanes : 0;
+    return SGMGB_OK;
+}
+
 int sgmgb_batch_set_fault(sgmgb_batch *b, int wait_limit_ms, int stall_frame) {
     if (!b || wait_limit_ms < 1 || wait_limit_ms > 600000 || stall_frame < -1 || stall_frame >= b->n)
         return SGMGB_ERR_ARG;
@@ -717,6 +899,7 @@ void sgmgb_batch_destroy(sgmgb_batch *b) {
     if (b->ctx) cudaSetDevice(b->ctx->device);
     if (b->ran && b->done_ev) cudaEventSynchronize(b->done_ev);
     free_tables(b);
+    free_lanes(b);
     if (b->arena) cudaFree(b->arena);
     if (b->h_frames) cudaFreeHost(b->h_frames);
     if (b->h_ctl) cudaFreeHost(b->h_ctl);

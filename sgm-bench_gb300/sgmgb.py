@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(BUILD, "libsgmgb.so")
 PLAIN, MULTISCALE = 0, 1
 POST_LR, POST_MEDIAN, POST_SUBPIXEL, DISP_INVALID = 1, 2, 4, 255
 SCHED_AUTO, SCHED_LATENCY, SCHED_THROUGHPUT, SCHED_FUSED, SCHED_SPLIT = 0, 1, 2, 3, 4
+BATCH_PERSISTENT, BATCH_IN_FLIGHT = 0, 1
 OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_NODEV, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 
 # every symbol include/sgmgb.h declares
@@ -36,7 +37,7 @@ EXPORTS = [
     "sgmgb_server_create", "sgmgb_server_add_camera", "sgmgb_server_submit", "sgmgb_server_poll",
     "sgmgb_server_wait", "sgmgb_server_stats_get", "sgmgb_server_destroy", "sgmgb_synth_pair",
     "sgmgb_server_prepare", "sgmgb_batch_busy", "sgmgb_run_frame_post",
-    "sgmgb_run_frame_noalloc",
+    "sgmgb_run_frame_noalloc", "sgmgb_batch_set_mode", "sgmgb_batch_mode",
 ]
 
 
@@ -108,6 +109,8 @@ def _load():
         "sgmgb_batch_tile_shape": (i, [vp, i, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "sgmgb_batch_busy": (i, [vp, ctypes.POINTER(ctypes.c_double), i, ctypes.POINTER(i)]),
         "sgmgb_batch_set_fault": (i, [vp, i, i]),
+        "sgmgb_batch_set_mode": (i, [vp, i, i]),
+        "sgmgb_batch_mode": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "sgmgb_batch_destroy": (None, [vp]),
         "sgmgb_tune_lookup": (i, [ctypes.c_char_p, fdp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "sgmgb_tune_record": (i, [ctypes.c_char_p, fdp, i, i, ctypes.c_double]),
@@ -311,7 +314,8 @@ class Engine:
 
 class Batch:
     """Many plain-variant frames of mixed shapes planned once and run as one
-    persistent launch (replayed as a CUDA graph)."""
+    persistent launch, or as frames in flight (set_mode), either replayed as a
+    CUDA graph."""
 
     def __init__(self, engine, descs, tune_cache=None):
         self.engine = engine
@@ -341,8 +345,8 @@ class Batch:
     BUSY_KINDS = ("census", "cost", "scratch", "final", "first_half_cost", "wait")
 
     def busy(self):
-        """Milliseconds the last run's blocks spent per work-item kind (summed
-        over blocks), and the block count under "blocks"."""
+        """Milliseconds the last persistent launch's blocks spent per work-item
+        kind (summed over blocks), and the block count under "blocks"."""
         out = (ctypes.c_double * 6)()
         nb = ctypes.c_int()
         self.engine._check(lib.sgmgb_batch_busy(self.h, out, 6, ctypes.byref(nb)))
@@ -358,6 +362,17 @@ class Batch:
 
     def set_fault(self, wait_limit_ms=2000, stall_frame=-1):
         self.engine._check(lib.sgmgb_batch_set_fault(self.h, wait_limit_ms, stall_frame))
+
+    def set_mode(self, mode, lanes=6):
+        """BATCH_PERSISTENT (one persistent launch) or BATCH_IN_FLIGHT (every
+        frame's own pipeline on `lanes` concurrent chains, one CUDA graph)."""
+        self.engine._check(lib.sgmgb_batch_set_mode(self.h, mode, lanes))
+
+    def mode(self):
+        """(mode, lanes); lanes is 0 in the persistent mode."""
+        m, k = ctypes.c_int(), ctypes.c_int()
+        self.engine._check(lib.sgmgb_batch_mode(self.h, ctypes.byref(m), ctypes.byref(k)))
+        return m.value, k.value
 
     def close(self):
         if self.h:

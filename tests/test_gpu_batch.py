@@ -1,4 +1,5 @@
-"""The batched form: many frames of mixed shapes in one persistent launch.
+"""The batched form: many frames of mixed shapes in one persistent launch, or
+as frames in flight in one CUDA graph.
 
 Every frame of a batch must equal the oracle (common/sgm_ref.c restated in
 oracle/sgm_oracle.c) byte for byte, on the first run and on graph replays with
@@ -74,6 +75,42 @@ def test_batch_new_buffers_each_run(engine):
     b.close()
 
 
+def test_batch_in_flight_mode_exact(engine):
+    """SGMGB_BATCH_IN_FLIGHT: every frame's own pipeline on concurrent chains,
+    one CUDA graph; maps equal the oracle's, on a replay and after new output
+    buffers (a new capture), and the persistent mode runs after it."""
+    import torch
+    descs, host, dev, outs = _frames(MIX, seed0=60)
+    b = sgmgb.Batch(engine, descs)
+    assert b.mode() == (sgmgb.BATCH_PERSISTENT, 0)
+    with pytest.raises(sgmgb.SgmError):
+        b.busy()                                   # no persistent launch yet
+    b.set_mode(sgmgb.BATCH_IN_FLIGHT, 3)
+    assert b.mode() == (sgmgb.BATCH_IN_FLIGHT, 3)
+    L, R = [d[0] for d in dev], [d[1] for d in dev]
+    for tag in ("first run: ", "replay: "):
+        for o in outs:
+            o.zero_()
+        b.run(L, R, outs)
+        b.wait()
+        torch.cuda.synchronize()
+        _check(host, outs, descs, tag)
+    outs2 = [torch.zeros_like(o) for o in outs]
+    b.run(L, R, outs2)
+    b.wait()
+    torch.cuda.synchronize()
+    _check(host, outs2, descs, "new buffers: ")
+    b.set_mode(sgmgb.BATCH_PERSISTENT)
+    for o in outs:
+        o.zero_()
+    b.run(L, R, outs)
+    b.wait()
+    torch.cuda.synchronize()
+    _check(host, outs, descs, "persistent after in flight: ")
+    assert b.busy()["blocks"] > 0
+    b.close()
+
+
 def test_batch_autotune_and_cache(engine, tmp_path):
     import torch
     specs = [(320, 240, 64, 4), (256, 128, 128, 8), (320, 240, 64, 4)]
@@ -85,6 +122,8 @@ def test_batch_autotune_and_cache(engine, tmp_path):
     shapes = [b.tile_shape(i) for i in range(len(specs))]
     for w, d in shapes:
         assert w in (2, 4) and d in (0, 2, 4, 8)
+    mode, lanes = b.mode()
+    assert (mode, lanes) == (sgmgb.BATCH_PERSISTENT, 0) or (mode == sgmgb.BATCH_IN_FLIGHT and lanes in (4, 6, 8))
     for o in outs:
         o.zero_()
     b.run(L, R, outs)
@@ -130,13 +169,18 @@ def test_batch_rejects_bad_input(engine):
     b = sgmgb.Batch(engine, [sgmgb.desc(16, 16, 64, 4)])
     with pytest.raises(sgmgb.SgmError):
         b.run([0], [0], [0])
+    for mode, lanes in ((2, 4), (-1, 4), (sgmgb.BATCH_IN_FLIGHT, 0), (sgmgb.BATCH_IN_FLIGHT, 9)):
+        with pytest.raises(sgmgb.SgmError):
+            b.set_mode(mode, lanes)
+    assert b.mode() == (sgmgb.BATCH_PERSISTENT, 0)
     b.close()
 
 
 def test_batch_baseline_sizes(engine, baseline_frames):
     """One persistent launch over frames at the batched configuration's sizes
     (1920x1080 D=128 8-path, 1920x800 D=64 8-path, 1280x720 D=128 4-path),
-    every map byte for byte against the checker, on two runs."""
+    every map byte for byte against the checker, on two runs, then a run of
+    the frames-in-flight mode."""
     import torch
     keys = list(baseline_frames)
     descs = [sgmgb.desc(*k) for k in keys]
@@ -145,7 +189,9 @@ def test_batch_baseline_sizes(engine, baseline_frames):
     outs = [torch.zeros((k[1], k[0]), dtype=torch.uint8, device="cuda") for k in keys]
     b = sgmgb.Batch(engine, descs)
     try:
-        for run in range(2):
+        for run in range(3):
+            if run == 2:                          # the frames-in-flight mode on the same frames
+                b.set_mode(sgmgb.BATCH_IN_FLIGHT, 2)
             for o in outs:
                 o.zero_()
             b.run(dl, dr, outs)
