@@ -358,8 +358,8 @@ def test_rejects_bad_schedule(engine):
 
 @pytest.mark.parametrize("pin", ["in", "out", "both"])
 def test_pinned_host_buffers(engine, pin):
-    """Page-locked host buffers are read (images) and written (map) by the
-    kernels directly; the result is the same as through the copy engines."""
+    """Page-locked host buffers (images, map or both) give the same map as
+    pageable ones."""
     import torch
     def pinned(a):
         t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
